@@ -1,0 +1,205 @@
+/*
+ * madsdp_gpu.h -- C ABI of the GB300 (sm_103a) interior-point library for
+ * MadSDP.jl.  Plain pointers and sizes only; every call returns an int status
+ * (0 = ok, negative = usage or CUDA error, see msdp_last_error).
+ *
+ * The library replaces, for one batch of SDPs resident on one GPU, the
+ * per-iteration numerical work that MadSDP performs on the CPU:
+ *
+ *   msdp_batch_create       MadSDPSolver(model; components..., options...)
+ *                           src/solver.jl:87-160 (workspace allocation) and
+ *                           the model upload done by LowRankOpt.Model
+ *   msdp_batch_initialize   initialize!(solver), src/solver.jl:286-293
+ *                           (initial_point!, initialize_algorithm!)
+ *   msdp_batch_iterate      iterate! + update_termination!,
+ *                           src/primal_dual.jl:85-134, src/dual_centering.jl:266-303
+ *   msdp_batch_solve        solve!(solver), src/solver.jl:385-396
+ *   msdp_batch_get_stats    the fields read by SolverCore.solve!, src/moi.jl:53-72
+ *   msdp_batch_get_solution MOI.get(::Solver, ::LRO.Solution), src/moi.jl:76-78
+ *
+ * and, for the Newton-system identity tests of the reference
+ * (test/qr_schur.jl:16-66), component-granular entry points mirroring
+ * update_residuals! (src/step.jl:12-47), _prepare! + _factorize_schur!
+ * (src/primal_dual.jl:29-37,74-80), correction! (src/step.jl:128-136) and
+ * _solve_directions! (src/primal_dual.jl:40-54).
+ *
+ * Storage conventions: dense matrices are column-major n x n float64;
+ * constraint matrices are coordinate lists of full symmetric entries
+ * (both triangles).  Host buffers are borrowed for the duration of a call.
+ */
+#ifndef MADSDP_GPU_H
+#define MADSDP_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- component selectors (src/components.jl) ---------------------------- */
+enum msdp_algorithm { MSDP_PRIMAL_DUAL = 0, MSDP_DUAL_CENTERING = 1 };
+enum msdp_direction { MSDP_NT = 0, MSDP_HKM = 1 };
+enum msdp_step_length { MSDP_EIGEN_STEP = 0, MSDP_CHOLESKY_BACKTRACK = 1 };
+enum msdp_centering { MSDP_MEHROTRA = 0, MSDP_ADAPTIVE_MU = 1 };
+enum msdp_initial_point { MSDP_SCALED_IDENTITY = 0, MSDP_INITIAL_POINT = 1, MSDP_DUAL_SHIFT = 2 };
+enum msdp_schur_solver { MSDP_DENSE_CHOLESKY = 0, MSDP_MADNLP_SCHUR = 1, MSDP_QR_SCHUR = 2 };
+enum msdp_precision { MSDP_FP64 = 0, MSDP_MIXED = 1 };
+
+/* ---- statuses (MadNLP.Status values used by MadSDP, src/moi.jl:16-29) --- */
+enum msdp_status {
+  MSDP_SOLVE_SUCCEEDED = 1,
+  MSDP_SOLVED_TO_ACCEPTABLE_LEVEL = 2,
+  MSDP_SEARCH_DIRECTION_BECOMES_TOO_SMALL = 3,
+  MSDP_MAXIMUM_ITERATIONS_EXCEEDED = 5,
+  MSDP_MAXIMUM_WALLTIME_EXCEEDED = 6,
+  MSDP_INFEASIBLE_PROBLEM_DETECTED = 8,
+  MSDP_ERROR_IN_STEP_COMPUTATION = 11,
+  MSDP_USER_REQUESTED_STOP = 13,
+  MSDP_INITIAL = 100,
+  MSDP_REGULAR = 101
+};
+
+/* ---- return codes ---------------------------------------------------------- */
+enum msdp_error {
+  MSDP_OK = 0,
+  MSDP_ERR_INVALID_ARGUMENT = -1, /* ArgumentError of the reference        */
+  MSDP_ERR_CUDA = -2,
+  MSDP_ERR_OUT_OF_MEMORY = -3,
+  MSDP_ERR_UNSUPPORTED = -4,      /* combination not built into the kernel */
+  MSDP_ERR_INITIAL_POINT = -5     /* ErrorException of the reference       */
+};
+
+/* Components: mirror src/components.jl:30-300 with their default values. */
+typedef struct msdp_components {
+  int32_t algorithm;      /* msdp_algorithm     (PrimalDual)        */
+  int32_t direction;      /* msdp_direction     (NT)                */
+  int32_t step;           /* msdp_step_length   (EigenStep)         */
+  int32_t centering;      /* msdp_centering     (Mehrotra)          */
+  int32_t initial_point;  /* msdp_initial_point (ScaledIdentity)    */
+  int32_t schur;          /* msdp_schur_solver  (DenseCholesky)     */
+  int32_t precision;      /* msdp_precision     (FP64)              */
+  int32_t centering_max_iter; /* DualCentering, 50                  */
+  double tau;             /* EigenStep tau, 0.95                    */
+  double shrink;          /* CholeskyBacktrack, 0.8                 */
+  double boundary;        /* CholeskyBacktrack, 0.95                */
+  double sigma_exponent;  /* Mehrotra, 3                            */
+  double initial_ratio;   /* AdaptiveMu, 1/4                        */
+  double ratio;           /* AdaptiveMu, 1/2                        */
+  double scale;           /* ScaledIdentity(scale); <= 0: automatic */
+  double initial_shift;   /* DualShift, 1                           */
+  double max_shift;       /* DualShift, 1e10                        */
+  double dc_beta;         /* DualCentering beta, 0.2                */
+  double dc_delta;        /* DualCentering delta, 1                 */
+  double dc_A;            /* DualCentering A, 2; NaN: theoretical   */
+} msdp_components;
+
+/* Options: src/options.jl:3-15, plus the precision switch of MSDP_MIXED. */
+typedef struct msdp_options {
+  double tol;              /* 1e-7  */
+  int32_t max_iter;        /* 100   */
+  int32_t max_schur_reg;   /* 8     */
+  double max_wall_time;    /* 3600  */
+  double mu_min;           /* 1e-14 */
+  double regularize_schur; /* 1e-12 */
+  int32_t datasparsity;    /* 8 (accepted, constraint storage is chosen per problem) */
+  int32_t pad0;
+  double switch_tol;       /* MSDP_MIXED: FP32 iterations while max(inf_pr, inf_du, gap) > switch_tol */
+} msdp_options;
+
+/* One problem in the form of LowRankOpt.Model(C, A, b, d_lin, C_lin, sides). */
+typedef struct msdp_problem_desc {
+  int32_t nblocks, m, ns, pad0;
+  const int32_t* sides;          /* [nblocks]                                   */
+  const double* const* C;        /* [nblocks] -> n_i*n_i column-major            */
+  const int64_t* A_nnz;          /* [nblocks] number of full symmetric entries   */
+  const int32_t* const* A_con;   /* [nblocks] -> [nnz] constraint index (0-based) */
+  const int32_t* const* A_row;   /* [nblocks] -> [nnz] row                       */
+  const int32_t* const* A_col;   /* [nblocks] -> [nnz] column                    */
+  const double* const* A_val;    /* [nblocks] -> [nnz] value                     */
+  const double* b;               /* [m]                                         */
+  const double* d_lin;           /* [ns]                                        */
+  const double* C_lin;           /* [m*ns] column-major                          */
+} msdp_problem_desc;
+
+/* Iteration data of one problem (src/solver.jl:37-48, src/moi.jl:57-65). */
+typedef struct msdp_stats {
+  int32_t status, iter;
+  int32_t iter_fp32, iter_fp64;  /* iterations run in each precision */
+  double pobj, dobj;
+  double inf_pr, inf_du, gap;    /* gap = inf_compl                  */
+  double mu, sigma, alpha, beta;
+  double solve_ns;               /* device time from initialize to termination */
+  int32_t n_newton, n_predictor; /* DualCentering counters            */
+} msdp_stats;
+
+/* One row of the iteration log (src/solver.jl:367-383). */
+typedef struct msdp_iter_record {
+  double iter, pobj, dobj, inf_pr, inf_du, gap, mu, alpha, beta, phase;
+} msdp_iter_record;
+
+typedef struct msdp_context msdp_context;
+typedef struct msdp_batch msdp_batch;
+
+void msdp_default_components(msdp_components* c);
+void msdp_default_options(msdp_options* o);
+
+/* Context: one CUDA device and one stream. */
+int msdp_context_create(int device, msdp_context** ctx);
+int msdp_context_destroy(msdp_context* ctx);
+const char* msdp_last_error(const msdp_context* ctx);
+int msdp_device_count(void);
+
+/* A batch of problems solved together (one CTA per problem at a time).
+ * Uploads every problem and allocates every workspace; nothing is
+ * allocated afterwards. */
+int msdp_batch_create(msdp_context* ctx, const msdp_problem_desc* problems, int32_t nprob,
+                      const msdp_components* comp, const msdp_options* opt, msdp_batch** batch);
+int msdp_batch_destroy(msdp_batch* batch);
+/* Bytes of device memory the batch holds. */
+int64_t msdp_batch_device_bytes(const msdp_batch* batch);
+
+/* InitialPoint(X, y; x) of problem `prob` (src/components.jl:286-294); x may be NULL. */
+int msdp_batch_set_initial_point(msdp_batch* batch, int32_t prob, const double* const* X,
+                                 const double* y, const double* x);
+/* Overwrite the iterate (X, S per block, y, x, z); NULL pointers keep the current value. */
+int msdp_batch_set_iterate(msdp_batch* batch, int32_t prob, const double* const* X,
+                           const double* const* S, const double* y, const double* x, const double* z);
+
+int msdp_batch_initialize(msdp_batch* batch);
+/* Run up to `max_iterations` iterations (<= 0: until every problem stops). */
+int msdp_batch_iterate(msdp_batch* batch, int32_t max_iterations);
+int msdp_batch_solve(msdp_batch* batch);
+int msdp_batch_synchronize(msdp_batch* batch);
+
+int msdp_batch_get_stats(msdp_batch* batch, int32_t prob, msdp_stats* out);
+int msdp_batch_get_all_stats(msdp_batch* batch, msdp_stats* out /* [nprob] */);
+/* X per block (n_i*n_i each), y (m), x (ns), z (ns); NULL pointers are skipped. */
+int msdp_batch_get_solution(msdp_batch* batch, int32_t prob, double* const* X, double* y,
+                            double* x, double* z);
+int msdp_batch_get_trajectory(msdp_batch* batch, int32_t prob, msdp_iter_record* out,
+                              int32_t capacity, int32_t* count);
+
+/* Component-granular steps (identity tests). */
+int msdp_batch_update_residuals(msdp_batch* batch);
+int msdp_batch_prepare(msdp_batch* batch, int32_t* ok /* [nprob]: _prepare! && _factorize_schur! */);
+int msdp_batch_solve_directions(msdp_batch* batch, double mu, int32_t corrected);
+int msdp_batch_correction(msdp_batch* batch);
+/* delX, delS per block; dely (m); delx, delz (ns); Rp (m); Rd per block. */
+int msdp_batch_get_directions(msdp_batch* batch, int32_t prob, double* const* delX,
+                              double* const* delS, double* dely, double* delx, double* delz);
+int msdp_batch_get_residuals(msdp_batch* batch, int32_t prob, double* Rp, double* const* Rd,
+                             double* Rd_lin);
+/* The NT scaling W and the correction of each block (n_i*n_i each). */
+int msdp_batch_get_block_matrix(msdp_batch* batch, int32_t prob, int32_t block, int32_t which,
+                                double* out);
+enum msdp_block_matrix { MSDP_MAT_W = 0, MSDP_MAT_CORR = 1, MSDP_MAT_SI = 2, MSDP_MAT_S = 3,
+                         MSDP_MAT_X = 4 };
+
+/* Number of kernel launches issued by this batch since creation. */
+int64_t msdp_batch_launch_count(const msdp_batch* batch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MADSDP_GPU_H */

@@ -1,0 +1,933 @@
+// The interior-point iteration of MadSDP as CTA-cooperative device code.
+//
+// One CTA owns one problem at a time and runs its whole iteration: the
+// block factorizations and NT/HKM scalings, the Schur complement assembly,
+// its Cholesky factorization and solves, the directions, the step lengths
+// and the update.  Each function names the reference function it follows
+// (paths relative to blegat/MadSDP.jl).
+//
+// The iterate (X, S, y, x, z), the residuals and every quantity that enters
+// a residual or an objective are float64.  The template parameter T is the
+// type of the block linear algebra (factorizations, scalings, E(.), the
+// Schur matrix): double for the FP64 path, float for the FP32 phase of the
+// mixed path.
+#pragma once
+#include "la.cuh"
+#include "layout.h"
+
+#ifndef MSDP_SMEM_BYTES
+#define MSDP_SMEM_BYTES (200 * 1024)
+#endif
+
+// Device code of one translation unit: internal linkage.
+namespace {
+
+struct SharedState {
+  RedBuf rb;
+  int flag;
+  int counter;
+  int prob;
+  int pad;
+  double bc[8];  // broadcast scalars
+};
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// ------------------------------------------------------------------ views
+struct Prob {
+  int p, nblocks, m, ns;
+  double *b, *y, *dely, *Rp, *h, *wm, *wm2, *dcd, *dcg, *dcgz, *dcdy, *dcyhat;
+  double *dlin, *x, *z, *delx, *delz, *Rdlin, *zinv, *corrlin, *ws, *ws2;
+  double* Clin;  // m x ns column-major
+  const double* norms;  // ||b||_inf, ||d_lin||_inf, max_i ||C_i||_inf
+  double* sc;
+  double* H64;
+  float *Hf, *Lf;
+  double* traj;
+  int ntraj;
+};
+
+__device__ __forceinline__ Prob make_prob(const BatchDev& B, int p) {
+  const ProbDesc& d = B.prob[p];
+  Prob P;
+  P.p = p; P.nblocks = d.nblocks; P.m = d.m; P.ns = d.ns;
+  double* v = B.d64 + d.v64;
+  const int m = d.m, ns = d.ns;
+  const double* dat = B.dd + d.bdat;
+  P.b = const_cast<double*>(dat);
+  P.dlin = const_cast<double*>(dat + m);
+  P.Clin = const_cast<double*>(dat + m + ns);
+  P.norms = dat + m + ns + (int64_t)m * ns;
+  P.y = v + (int64_t)V_Y * m; P.dely = v + (int64_t)V_DELY * m;
+  P.Rp = v + (int64_t)V_RP * m; P.h = v + (int64_t)V_H * m; P.wm = v + (int64_t)V_WM * m;
+  P.wm2 = v + (int64_t)V_WM2 * m; P.dcd = v + (int64_t)V_DCD * m; P.dcg = v + (int64_t)V_DCG * m;
+  P.dcgz = v + (int64_t)V_DCGZ * m; P.dcdy = v + (int64_t)V_DCDY * m; P.dcyhat = v + (int64_t)V_DCYHAT * m;
+  double* s = v + (int64_t)V_MCOUNT * m;
+  P.x = s + (int64_t)S_X * ns; P.z = s + (int64_t)S_Z * ns;
+  P.delx = s + (int64_t)S_DELX * ns; P.delz = s + (int64_t)S_DELZ * ns; P.Rdlin = s + (int64_t)S_RDLIN * ns;
+  P.zinv = s + (int64_t)S_ZINV * ns; P.corrlin = s + (int64_t)S_CORR * ns; P.ws = s + (int64_t)S_WS * ns;
+  P.ws2 = s + (int64_t)S_WS2 * ns;
+  P.sc = s + (int64_t)S_COUNT * ns;
+  P.H64 = B.d64 + d.H64;
+  P.Hf = d.Hf >= 0 ? B.d32 + d.Hf : nullptr;
+  P.Lf = d.Lf >= 0 ? B.d32 + d.Lf : nullptr;
+  P.traj = B.d64 + d.traj;
+  P.ntraj = d.ntraj;
+  return P;
+}
+
+template <class T>
+struct Blk {
+  int n;
+  int64_t nn;
+  double *C, *base, *X, *S, *Rd, *dX, *dS, *buf, *ATy, *Shat, *Dc, *bsc;
+  T* w;
+  int64_t nnz;
+  const int32_t *erow, *ecol, *pcon;
+  const double *eval, *pval;
+  const int64_t *cptr, *pptr;
+  double cnorm;
+  __device__ __forceinline__ T* W(int k) const { return w + (int64_t)k * nn; }
+  __device__ __forceinline__ T* V(int k) const { return w + (int64_t)W_COUNT * nn + (int64_t)k * (n + 1); }
+  __device__ __forceinline__ double* M(int k) const { return base + (int64_t)k * nn; }
+};
+
+template <class T> __device__ __forceinline__ T* wbase(const BatchDev& B, const BlockDesc& d);
+template <> __device__ __forceinline__ double* wbase<double>(const BatchDev& B, const BlockDesc& d) { return B.d64 + d.w64; }
+template <> __device__ __forceinline__ float* wbase<float>(const BatchDev& B, const BlockDesc& d) { return B.d32 + d.w32; }
+
+template <class T>
+__device__ __forceinline__ Blk<T> make_blk(const BatchDev& B, const Prob& P, int i) {
+  const BlockDesc& d = B.blk[B.prob[P.p].blk0 + i];
+  Blk<T> b;
+  b.n = d.n; b.nn = (int64_t)d.n * d.n;
+  b.C = const_cast<double*>(B.dd + d.cdat);
+  b.base = B.d64 + d.m64;
+  b.X = b.M(M_X); b.S = b.M(M_S); b.Rd = b.M(M_RD); b.dX = b.M(M_DX); b.dS = b.M(M_DS);
+  b.buf = b.M(M_BUF); b.ATy = b.M(M_ATY); b.Shat = b.M(M_SHAT); b.Dc = b.M(M_DC);
+  b.bsc = b.base + (int64_t)M_COUNT * b.nn;
+  b.w = wbase<T>(B, d);
+  b.nnz = d.nnz;
+  b.erow = B.e_row + d.ent; b.ecol = B.e_col + d.ent; b.eval = B.e_val + d.ent;
+  b.pcon = B.p_con + d.ent; b.pval = B.p_val + d.ent;
+  b.cptr = B.ptr + d.conptr; b.pptr = B.ptr + d.posptr;
+  b.cnorm = d.cnorm;
+  return b;
+}
+
+// "T view" of a float64 array: the array itself for T = double, else a
+// converted copy in `slot`.
+template <class T> __device__ __forceinline__ T* as_T(int64_t len, const double* src, T* slot);
+template <> __device__ __forceinline__ double* as_T<double>(int64_t, const double* src, double*) {
+  return const_cast<double*>(src);
+}
+template <> __device__ __forceinline__ float* as_T<float>(int64_t len, const double* src, float* slot) {
+  cta_convert<float, double>(len, slot, src);
+  return slot;
+}
+
+// ------------------------------------------------------------------ A(.) and A*(.)
+// out[j] += <A_ij, X_i> (LowRankOpt.add_jprod!, src/step.jl:19)
+template <class T, class U>
+__device__ void jprod_add(const Blk<T>& b, int m, const U* X, double* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j = warp; j < m; j += NWARPS) {
+    const int64_t s = b.cptr[j], e = b.cptr[j + 1];
+    double acc = 0.0;
+    for (int64_t q = s + lane; q < e; q += 32)
+      acc = fma(b.eval[q], (double)X[b.erow[q] + (int64_t)b.ecol[q] * b.n], acc);
+    acc = warp_sum(acc);
+    if (lane == 0) out[j] += acc;
+  }
+  __syncthreads();
+}
+
+// out = base1 - base2 + sgn * A_i*(y) (LowRankOpt.unsafe_jtprod, src/step.jl:30).
+template <class T>
+__device__ void jtprod_combine(const Blk<T>& b, const double* y, double sgn, const double* base1,
+                               const double* base2, double* out) {
+  for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) {
+    double s = 0.0;
+    const int64_t q1 = b.pptr[k + 1];
+    for (int64_t q = b.pptr[k]; q < q1; ++q) s = fma(y[b.pcon[q]], b.pval[q], s);
+    double v = base1 ? base1[k] : 0.0;
+    if (base2) v -= base2[k];
+    out[k] = v + sgn * s;
+  }
+  __syncthreads();
+}
+
+// out += sgn * C_lin * v   (m)      /   out = base + sgn * C_lin' v  (ns)
+__device__ void clin_mv(const Prob& P, const double* v, double sgn, double* out) {
+  for (int j = threadIdx.x; j < P.m; j += NTHREADS) {
+    double s = 0.0;
+    for (int k = 0; k < P.ns; ++k) s = fma(P.Clin[j + (int64_t)k * P.m], v[k], s);
+    out[j] += sgn * s;
+  }
+  __syncthreads();
+}
+__device__ void clin_tmv(const Prob& P, const double* v, const double* base, double sgn, double* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = warp; k < P.ns; k += NWARPS) {
+    double s = 0.0;
+    for (int j = lane; j < P.m; j += 32) s = fma(P.Clin[j + (int64_t)k * P.m], v[j], s);
+    s = warp_sum(s);
+    if (lane == 0) out[k] = (base ? base[k] : 0.0) + sgn * s;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ block helpers
+// L = chol(sym(M)) with the flush of src/blocks.jl:94-113 (flush = true),
+// or a plain positive-definiteness test (out = nullptr).
+template <class T, class U>
+__device__ bool chol_factor(int n, const U* M, T* out, bool flush, unsigned char* smem, SharedState& sh) {
+  const int64_t nn = (int64_t)n * n;
+  T* A = (nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) ? (T*)smem : out;
+  cta_sym_copy<T, U>(n, A, M);
+  if (!cta_potrf<T>(n, A, n, &sh.flag)) return false;
+  if (out == nullptr) return true;
+  if (flush) cta_flush_lower<T>(n, A, n, &sh.rb);
+  if (A != out) {
+    for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) out[k] = A[k];
+    __syncthreads();
+  }
+  return true;
+}
+
+// Whether X + a dX is positive definite (src/blocks.jl:133-137); `work` is
+// an n x n T buffer used when shared memory is too small.
+template <class T>
+__device__ bool add_mul_posdef(int n, const double* X, double a, const double* dX, T* work,
+                               unsigned char* smem, SharedState& sh) {
+  const int64_t nn = (int64_t)n * n;
+  T* A = (nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) ? (T*)smem : work;
+  for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) A[k] = (T)(X[k] + a * dX[k]);
+  __syncthreads();
+  return cta_potrf<T>(n, A, n, &sh.flag);
+}
+
+template <class T>
+__device__ void tri_inverse(int n, const T* L, T* Li, unsigned char* smem) {
+  const int64_t nn = (int64_t)n * n;
+  if (2 * nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) {
+    T* sL = (T*)smem;
+    T* sLi = sL + nn;
+    for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) sL[k] = L[k];
+    __syncthreads();
+    cta_trtri_lower<T>(n, sL, sLi);
+    for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) Li[k] = sLi[k];
+    __syncthreads();
+  } else {
+    cta_trtri_lower<T>(n, L, Li);
+  }
+}
+
+// ------------------------------------------------------------------ Lanczos
+// Smallest eigenvalue of the symmetric Z (n x n) by Lanczos with full
+// reorthogonalization (the role of LowRankOpt.lanczos_eigmin!,
+// src/step.jl:151-183).  Q (n x n) holds the basis; a, bb, w, coef are
+// vectors of length n+1.  Stops when the smallest Ritz value is stable or
+// the Krylov space is exhausted.
+template <class T>
+__device__ T lanczos_eigmin(int n, const T* Z, T* Q, T* a, T* bb, T* w, T* coef, SharedState& sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // deterministic pseudo-random start vector
+  double nrm2 = 0.0;
+  for (int i = threadIdx.x; i < n; i += NTHREADS) {
+    uint32_t hsh = (uint32_t)(i + 1) * 2654435761u;
+    hsh ^= hsh >> 15; hsh *= 2246822519u; hsh ^= hsh >> 13;
+    const T v = (T)((double)(hsh & 0xffffff) / 16777216.0 - 0.5) + (T)0.01;
+    Q[i] = v;
+    nrm2 += (double)v * v;
+  }
+  nrm2 = block_sum(nrm2, &sh.rb);
+  {
+    const T inv = (T)(1.0 / sqrt(nrm2));
+    for (int i = threadIdx.x; i < n; i += NTHREADS) Q[i] *= inv;
+    __syncthreads();
+  }
+  T theta = (T)0, theta_prev = (T)INFINITY;
+  T znorm = (T)0;
+  int k = 0;
+  for (int j = 0; j < n; ++j) {
+    const T* qj = Q + (int64_t)j * n;
+    // w = Z q_j (Z symmetric: w_i = column i . q_j)
+    for (int i = warp; i < n; i += NWARPS) {
+      const T* zi = Z + (int64_t)i * n;
+      T s = 0;
+      for (int r = lane; r < n; r += 32) s = fma(zi[r], qj[r], s);
+      s = warp_sum(s);
+      if (lane == 0) w[i] = s;
+    }
+    __syncthreads();
+    double aj = 0.0;
+    for (int i = threadIdx.x; i < n; i += NTHREADS) aj += (double)qj[i] * w[i];
+    aj = block_sum(aj, &sh.rb);
+    if (threadIdx.x == 0) a[j] = (T)aj;
+    {
+      const T* qp = j > 0 ? Q + (int64_t)(j - 1) * n : nullptr;
+      const T bj = j > 0 ? bb[j] : (T)0;
+      for (int i = threadIdx.x; i < n; i += NTHREADS) {
+        T v = w[i] - (T)aj * qj[i];
+        if (qp) v -= bj * qp[i];
+        w[i] = v;
+      }
+      __syncthreads();
+    }
+    // full reorthogonalization, twice
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int l = warp; l <= j; l += NWARPS) {
+        const T* ql = Q + (int64_t)l * n;
+        T s = 0;
+        for (int r = lane; r < n; r += 32) s = fma(ql[r], w[r], s);
+        s = warp_sum(s);
+        if (lane == 0) coef[l] = s;
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += NTHREADS) {
+        T v = w[i];
+        for (int l = 0; l <= j; ++l) v = fma(-coef[l], Q[i + (int64_t)l * n], v);
+        w[i] = v;
+      }
+      __syncthreads();
+    }
+    double bn = 0.0;
+    for (int i = threadIdx.x; i < n; i += NTHREADS) bn += (double)w[i] * w[i];
+    bn = sqrt(block_sum(bn, &sh.rb));
+    k = j + 1;
+    if (threadIdx.x == 0) {
+      znorm = fmax(znorm, fabs(a[j]) + (T)bn + (j > 0 ? fabs(bb[j]) : (T)0));
+      if (j + 1 <= n) bb[j + 1] = (T)bn;
+    }
+    // broadcast znorm through shared memory
+    if (threadIdx.x == 0) sh.bc[0] = (double)znorm;
+    __syncthreads();
+    znorm = (T)sh.bc[0];
+    const bool exhausted = (k == n) || !(bn > (double)Num<T>::eps() * (double)znorm * 4.0);
+    const bool check = exhausted || (k >= 4 && (k % 4) == 0);
+    if (check) {
+      if (warp == 0) {
+        const T th = warp_tridiag_eigmin<T>(k, a, bb);
+        if (lane == 0) sh.bc[1] = (double)th;
+      }
+      __syncthreads();
+      theta = (T)sh.bc[1];
+      __syncthreads();
+      const T tolr = (T)(Num<T>::eps() * 64) * fmax((T)1, fabs(theta));
+      if (exhausted || fabs(theta - theta_prev) <= tolr) break;
+      theta_prev = theta;
+    }
+    // q_{j+1} = w / b_{j+1}
+    T* qn = Q + (int64_t)(j + 1) * n;
+    const T inv = (T)(1.0 / bn);
+    for (int i = threadIdx.x; i < n; i += NTHREADS) qn[i] = w[i] * inv;
+    __syncthreads();
+  }
+  return theta;
+}
+
+// ------------------------------------------------------------------ algorithm
+template <class T>
+struct Algo {
+  const BatchDev& B;
+  const Params& prm;
+  Prob& P;
+  unsigned char* smem;
+  SharedState& sh;
+
+  __device__ Algo(const BatchDev& B_, Prob& P_, unsigned char* smem_, SharedState& sh_)
+      : B(B_), prm(B_.prm), P(P_), smem(smem_), sh(sh_) {}
+
+  __device__ __forceinline__ Blk<T> blk(int i) const { return make_blk<T>(B, P, i); }
+  __device__ __forceinline__ int nu() const {
+    int s = P.ns;
+    for (int i = 0; i < P.nblocks; ++i) s += B.blk[B.prob[P.p].blk0 + i].n;
+    return s;
+  }
+  // X in the compute type: X itself for double, the converted copy for float
+  __device__ __forceinline__ const T* xt(const Blk<T>& b) const;
+  __device__ __forceinline__ bool is_nt() const {
+    return prm.algorithm == MSDP_PRIMAL_DUAL && prm.direction == MSDP_NT;
+  }
+
+  // ---------------- residuals (src/step.jl:12-47)
+  __noinline__ __device__ void update_residuals() {
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.Rp[j] = 0.0;
+    __syncthreads();
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      jprod_add(b, P.m, b.X, P.Rp);
+    }
+    if (P.ns > 0) clin_mv(P, P.x, 1.0, P.Rp);
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.Rp[j] = P.b[j] - P.Rp[j];
+    __syncthreads();
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      jtprod_combine(b, P.y, -1.0, b.C, b.S, b.Rd);
+      double mx = 0.0;
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) mx = fmax(mx, fabs(b.Rd[k]));
+      mx = block_max(mx, &sh.rb);
+      if (threadIdx.x == 0) b.bsc[BS_RDNZ] = (mx > 100.0 * 2.220446049250313e-16 * fmax(1.0, b.cnorm)) ? 1.0 : 0.0;
+      __syncthreads();
+    }
+    if (P.ns > 0) {
+      clin_tmv(P, P.y, nullptr, 1.0, P.Rdlin);
+      for (int k = threadIdx.x; k < P.ns; k += NTHREADS) P.Rdlin[k] = P.dlin[k] - P.z[k] - P.Rdlin[k];
+      __syncthreads();
+    }
+  }
+
+  __device__ double total_complementarity() {
+    double s = 0.0;
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      double t = 0.0;
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) t = fma(b.X[k], b.S[k], t);
+      s += block_sum(t, &sh.rb);
+    }
+    if (P.ns > 0) {
+      double t = 0.0;
+      for (int k = threadIdx.x; k < P.ns; k += NTHREADS) t = fma(P.x[k], P.z[k], t);
+      s += block_sum(t, &sh.rb);
+    }
+    return s;
+  }
+
+  // ---------------- S = sym(C - A*(y)), z = d - C_lin' y (src/solver.jl:192-211)
+  __device__ void slack(const Blk<T>& b, const double* y, double* out) {
+    jtprod_combine(b, y, -1.0, b.C, nullptr, out);
+    cta_symmetrize<double>(b.n, out);
+  }
+  __device__ void set_dual_slacks() {
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      slack(b, P.y, b.S);
+    }
+    if (P.ns > 0) clin_tmv(P, P.y, P.dlin, -1.0, P.z);
+  }
+
+  // ---------------- _prepare! (src/primal_dual.jl:29-37)
+  __device__ bool prepare_block(const Blk<T>& b) {
+    // src/blocks.jl:126-130: Ls = chol(S) with flush, Si = S^-1
+    if (!chol_factor<T, double>(b.n, b.S, b.W(W_LS), true, smem, sh)) return false;
+    tri_inverse<T>(b.n, b.W(W_LS), b.W(W_LSI), smem);
+    // Si = Ls^-T Ls^-1 (potri)
+    cta_gemm<T>(b.n, 1, 0, 1, 1, (T)1, b.W(W_LSI), b.W(W_LSI), (T)0, b.W(W_SI));
+    cta_symmetrize<T>(b.n, b.W(W_SI));
+    return true;
+  }
+
+  // NT scaling (src/directions.jl:45-75): Lx, M = Ls' Lx, SVD of M by
+  // one-sided Jacobi (M V = U diag(D), so N = M'M = V diag(D)^2 V'),
+  // G = Lx V D^-1/2, Gi = D^1/2 V' Lx^-1, W = G G'.
+  __noinline__ __device__ bool prepare_nt(const Blk<T>& b) {
+    const int n = b.n;
+    const int64_t nn = b.nn;
+    T* M = b.W(W_T1);
+    T* V = b.W(W_T2);
+    T* D = b.V(WV_D);
+    cta_gemm<T>(n, 1, 0, 1, 1, (T)1, b.W(W_LS), b.W(W_LX), (T)0, M);
+    bool conv;
+    if (2 * nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) {
+      T* sM = (T*)smem;
+      T* sV = sM + nn;
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) sM[k] = M[k];
+      __syncthreads();
+      conv = cta_jacobi_svd<T>(n, sM, sV, D, 40, &sh.counter);
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) V[k] = sV[k];
+      __syncthreads();
+    } else {
+      conv = cta_jacobi_svd<T>(n, M, V, D, 40, &sh.counter);
+    }
+    if (threadIdx.x == 0) {
+      int bad = conv ? 0 : 1;
+      for (int k = 0; k < n; ++k)
+        if (!(D[k] > (T)0) || !Num<T>::finite(D[k])) bad = 1;
+      sh.flag = bad;
+    }
+    __syncthreads();
+    if (sh.flag) return false;
+    // G = Lx V, then column scaling by D^-1/2
+    cta_gemm<T>(n, 0, 0, 1, 0, (T)1, b.W(W_LX), V, (T)0, b.W(W_G));
+    // Gi = V' Lx^-1, then row scaling by D^1/2
+    cta_gemm<T>(n, 1, 0, 0, 1, (T)1, V, b.W(W_LXI), (T)0, b.W(W_GI));
+    {
+      T* G = b.W(W_G);
+      T* Gi = b.W(W_GI);
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+        const int i = (int)(k % n), j = (int)(k / n);
+        G[k] = G[k] / Num<T>::sqrt_(D[j]);
+        Gi[k] = Gi[k] * Num<T>::sqrt_(D[i]);
+      }
+      __syncthreads();
+    }
+    cta_gemm<T>(n, 0, 1, 0, 0, (T)1, b.W(W_G), b.W(W_G), (T)0, b.W(W_W));
+    cta_symmetrize<T>(n, b.W(W_W));
+    return true;
+  }
+
+  __noinline__ __device__ bool prepare() {
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      if (!prepare_block(b)) return false;
+      const bool need_lx = is_nt() || prm.step == MSDP_EIGEN_STEP;
+      if (need_lx) {
+        // Lx = chol(X) (src/directions.jl:46 and src/step.jl:177; computed once)
+        if (!chol_factor<T, double>(b.n, b.X, b.W(W_LX), true, smem, sh)) return false;
+        tri_inverse<T>(b.n, b.W(W_LX), b.W(W_LXI), smem);
+      }
+      if (is_nt()) {
+        if (!prepare_nt(b)) return false;
+      }
+      // the compute-type view of X used by HKM's E(.) and Schur scaling
+      if (!is_nt()) (void)as_T<T>(b.nn, b.X, b.W(W_XT));
+    }
+    for (int k = threadIdx.x; k < P.ns; k += NTHREADS) P.zinv[k] = 1.0 / P.z[k];
+    __syncthreads();
+    return true;
+  }
+
+  // ---------------- Schur complement (LowRankOpt.schur_complement!)
+  // H_jk += <A_j, L A_k R> over the coordinate lists.  Only the (j >= k)
+  // half is computed; both halves are written.
+  __noinline__ __device__ void schur_block_add(const Blk<T>& b, const T* Lg, const T* Rg, T* H) {
+    const int n = b.n, m = P.m;
+    const int64_t nn = b.nn;
+    const T* L = Lg;
+    const T* R = Rg;
+    const int64_t need = (Lg == Rg ? 1 : 2) * nn * (int64_t)sizeof(T);
+    if (need <= MSDP_SMEM_BYTES) {
+      T* sL = (T*)smem;
+      T* sR = (Lg == Rg) ? sL : sL + nn;
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+        sL[k] = Lg[k];
+        if (Lg != Rg) sR[k] = Rg[k];
+      }
+      __syncthreads();
+      L = sL;
+      R = sR;
+    }
+    const int64_t mm = (int64_t)m * m;
+    for (int64_t idx = threadIdx.x; idx < mm; idx += NTHREADS) {
+      const int j = (int)(idx % m), k = (int)(idx / m);
+      if (j < k) continue;
+      const int64_t e0 = b.cptr[j], e1 = b.cptr[j + 1];
+      const int64_t f0 = b.cptr[k], f1 = b.cptr[k + 1];
+      T acc = (T)0;
+      for (int64_t e = e0; e < e1; ++e) {
+        const int re = b.erow[e], ce = b.ecol[e];
+        const T ve = (T)b.eval[e];
+        T part = (T)0;
+        for (int64_t f = f0; f < f1; ++f) {
+          const int rf = b.erow[f], cf = b.ecol[f];
+          part = fma((T)b.eval[f] * L[re + (int64_t)rf * n], R[cf + (int64_t)ce * n], part);
+        }
+        acc = fma(ve, part, acc);
+      }
+      H[j + (int64_t)k * m] += acc;
+      if (j != k) H[k + (int64_t)j * m] += acc;
+    }
+    __syncthreads();
+  }
+
+  __noinline__ __device__ void schur_complement(T* H) {
+    const int m = P.m;
+    const int64_t mm = (int64_t)m * m;
+    for (int64_t k = threadIdx.x; k < mm; k += NTHREADS) H[k] = (T)0;
+    __syncthreads();
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const T *L, *R;
+      if (prm.algorithm == MSDP_DUAL_CENTERING) { L = b.W(W_SI); R = b.W(W_SI); }
+      else if (prm.direction == MSDP_NT) { L = b.W(W_W); R = b.W(W_W); }
+      else { L = b.W(W_SI); R = xt(b); }
+      schur_block_add(b, L, R, H);
+    }
+    if (P.ns > 0) {
+      // + C_lin diag(x ./ z) C_lin' (scalar scalings x and 1 ./ z, src/solver.jl:30-31)
+      for (int k = threadIdx.x; k < P.ns; k += NTHREADS) P.ws2[k] = P.x[k] * P.zinv[k];
+      __syncthreads();
+      for (int64_t idx = threadIdx.x; idx < mm; idx += NTHREADS) {
+        const int j = (int)(idx % m), k = (int)(idx / m);
+        double s = 0.0;
+        for (int l = 0; l < P.ns; ++l)
+          s = fma(P.Clin[j + (int64_t)l * m] * P.ws2[l], P.Clin[k + (int64_t)l * m], s);
+        H[idx] = (T)((double)H[idx] + s);
+      }
+      __syncthreads();
+    }
+  }
+
+  // The Schur matrix and its factor for this compute type.
+  __device__ T* schur_H();
+  __device__ T* schur_L();
+
+  // factorize_schur! with the regularization retry loop (src/solver.jl:299-314)
+  __noinline__ __device__ bool factorize_schur() {
+    const int m = P.m;
+    const int64_t mm = (int64_t)m * m;
+    T* H = schur_H();
+    T* L = schur_L();
+    double reg = prm.regularize_schur;
+    for (int attempt = 0; attempt < prm.max_schur_reg; ++attempt) {
+      schur_complement(H);
+      if (reg > 0.0) {
+        for (int i = threadIdx.x; i < m; i += NTHREADS) H[i + (int64_t)i * m] += (T)reg;
+        __syncthreads();
+      }
+      T* A = (mm * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) ? (T*)smem : L;
+      if (A != H) {
+        for (int64_t k = threadIdx.x; k < mm; k += NTHREADS) A[k] = H[k];
+        __syncthreads();
+      }
+      bool ok = cta_potrf<T>(m, A, m, &sh.flag);
+      if (ok) {
+        if (A != L) {
+          for (int64_t k = threadIdx.x; k < mm; k += NTHREADS) L[k] = A[k];
+          __syncthreads();
+        }
+        return true;
+      }
+      reg = (reg == 0.0) ? 1e-12 : 10.0 * reg;
+    }
+    return false;
+  }
+
+  // x = H^-1 x (src/schur_solvers.jl:21); the float factor is followed by
+  // two steps of iterative refinement with float64 residuals.
+  __device__ void schur_solve(double* x);
+
+  // ---------------- E(.) (src/directions.jl:80-84,116-120)
+  __noinline__ __device__ void apply_E(const Blk<T>& b, const T* Min, T* out) {
+    const int n = b.n;
+    T* tmp = b.W(W_T3);
+    if (is_nt()) {
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_W), Min, (T)0, tmp);
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, tmp, b.W(W_W), (T)0, out);
+    } else {
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, xt(b), Min, (T)0, tmp);
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, tmp, b.W(W_SI), (T)0, out);
+    }
+    cta_symmetrize<T>(n, out);
+  }
+
+  // ---------------- rhs! (src/step.jl:63-89)
+  __noinline__ __device__ void rhs(double mu, bool corrected) {
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.h[j] = P.Rp[j];
+    __syncthreads();
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const bool rdnz = b.bsc[BS_RDNZ] != 0.0;
+      if (rdnz) {
+        T* rdt = as_T<T>(b.nn, b.Rd, b.W(W_T2));
+        apply_E(b, rdt, b.W(W_ERD));
+      }
+      const T* Si = b.W(W_SI);
+      const T* erd = b.W(W_ERD);
+      const T* corr = b.W(W_CORR);
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) {
+        double v = b.X[k] - mu * (double)Si[k];
+        if (rdnz) v += (double)erd[k];
+        if (corrected) v -= (double)corr[k];
+        b.buf[k] = v;
+      }
+      __syncthreads();
+      jprod_add(b, P.m, b.buf, P.h);
+    }
+    if (P.ns > 0) {
+      for (int k = threadIdx.x; k < P.ns; k += NTHREADS) {
+        const double x = P.x[k], zi = P.zinv[k];
+        double v = x - mu * zi + x * zi * P.Rdlin[k];
+        if (corrected) v -= P.corrlin[k];
+        P.ws[k] = v;
+      }
+      __syncthreads();
+      clin_mv(P, P.ws, 1.0, P.h);
+    }
+  }
+
+  // ---------------- directions! (src/step.jl:94-124)
+  __noinline__ __device__ void directions(double mu, bool corrected) {
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const bool rdnz = b.bsc[BS_RDNZ] != 0.0;
+      // A*(dely), and dS = sym(Rd - A*(dely))
+      jtprod_combine(b, P.dely, 1.0, nullptr, nullptr, b.ATy);
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) b.dS[k] = b.Rd[k] - b.ATy[k];
+      __syncthreads();
+      cta_symmetrize<double>(b.n, b.dS);
+      T* at = as_T<T>(b.nn, b.ATy, b.W(W_T2));
+      apply_E(b, at, b.W(W_T1));
+      const T* Si = b.W(W_SI);
+      const T* e1 = b.W(W_T1);
+      const T* erd = b.W(W_ERD);
+      const T* corr = b.W(W_CORR);
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) {
+        double v = mu * (double)Si[k] - b.X[k] + (double)e1[k];
+        if (rdnz) v -= (double)erd[k];
+        if (corrected) v += (double)corr[k];
+        b.dX[k] = v;
+      }
+      __syncthreads();
+      cta_symmetrize<double>(b.n, b.dX);
+    }
+    if (P.ns > 0) {
+      clin_tmv(P, P.dely, P.Rdlin, -1.0, P.delz);
+      for (int k = threadIdx.x; k < P.ns; k += NTHREADS) {
+        const double x = P.x[k], zi = P.zinv[k];
+        double v = mu * zi - x - x * zi * P.delz[k];
+        if (corrected) v += P.corrlin[k];
+        P.delx[k] = v;
+      }
+      __syncthreads();
+    }
+  }
+
+  // ---------------- correction! (src/step.jl:128-136, src/directions.jl:90-100,123-127)
+  __noinline__ __device__ void correction() {
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const int n = b.n;
+      T* dxt = as_T<T>(b.nn, b.dX, b.W(W_DXT));
+      T* dst = as_T<T>(b.nn, b.dS, b.W(W_DST));
+      T* t1 = b.W(W_T1);
+      T* t2 = b.W(W_T2);
+      T* t3 = b.W(W_T3);
+      T* corr = b.W(W_CORR);
+      if (is_nt()) {
+        T* RNT = b.W(W_RNT);
+        const T* D = b.V(WV_D);
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_GI), dxt, (T)0, t1);
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, t1, dst, (T)0, t2);
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, t2, b.W(W_G), (T)0, t3);
+        for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) {
+          const int p = (int)(k % n), q = (int)(k / n);
+          RNT[k] = -(t3[k] + t3[q + (int64_t)p * n]) / (D[p] + D[q]);
+        }
+        __syncthreads();
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_G), RNT, (T)0, t1);
+        cta_gemm<T>(n, 0, 1, 0, 0, (T)1, t1, b.W(W_G), (T)0, corr);
+      } else {
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, dxt, dst, (T)0, t1);
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)-1, t1, b.W(W_SI), (T)0, corr);
+      }
+      cta_symmetrize<T>(n, corr);
+    }
+    for (int k = threadIdx.x; k < P.ns; k += NTHREADS) P.corrlin[k] = -P.delx[k] * P.delz[k] * P.zinv[k];
+    __syncthreads();
+  }
+
+  // ---------------- step lengths (src/step.jl:148-228)
+  __device__ double max_scalar_step(const double* x, const double* dx) {
+    double a = INFINITY;
+    for (int k = threadIdx.x; k < P.ns; k += NTHREADS)
+      if (dx[k] < 0.0) a = fmin(a, -x[k] / dx[k]);
+    // min reduction via max of negatives
+    return -block_max(-a, &sh.rb);
+  }
+
+  // Fraction tau of the largest step keeping L L' + a D positive definite,
+  // from the smallest eigenvalue of L^-1 D L^-T (src/step.jl:178-183).
+  __noinline__ __device__ double eigen_step(const Blk<T>& b, const T* Li, const double* Dm, double tau) {
+    const int n = b.n;
+    T* dt = as_T<T>(b.nn, Dm, b.W(W_DXT));
+    T* t1 = b.W(W_T1);
+    T* Z = b.W(W_T2);
+    cta_gemm<T>(n, 0, 0, 1, 0, (T)1, Li, dt, (T)0, t1);
+    cta_gemm<T>(n, 0, 1, 0, 1, (T)1, t1, Li, (T)0, Z);
+    const T* Zs = Z;
+    const int64_t nn = b.nn;
+    if (nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) {
+      T* sZ = (T*)smem;
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) sZ[k] = Z[k];
+      __syncthreads();
+      Zs = sZ;
+    }
+    const T lam = lanczos_eigmin<T>(n, Zs, b.W(W_Q), b.V(WV_LA), b.V(WV_LB), b.V(WV_LW), b.V(WV_LC), sh);
+    const double l = (double)lam;
+    return l > -sqrt(2.220446049250313e-16) ? 1.0 : fmin(1.0, -tau / l);
+  }
+
+  __noinline__ __device__ double backtrack(bool primal) {
+    double a = 1.0;
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const double* X = primal ? b.X : b.S;
+      const double* dX = primal ? b.dX : b.dS;
+      int trials = 0;
+      while (!add_mul_posdef<T>(b.n, X, a, dX, b.W(W_T1), smem, sh)) {
+        a *= prm.shrink;
+        if (a < 2.220446049250313e-16 || ++trials > 4096) return 0.0;
+      }
+    }
+    if (a != 1.0) a *= prm.boundary;
+    if (P.ns > 0) a = fmin(a, prm.boundary * max_scalar_step(primal ? P.x : P.z, primal ? P.delx : P.delz));
+    return a;
+  }
+
+  __device__ void step_lengths(double& a, double& bt) {
+    if (prm.step == MSDP_EIGEN_STEP) {
+      a = 1.0; bt = 1.0;
+      for (int i = 0; i < P.nblocks; ++i) {
+        Blk<T> b = blk(i);
+        a = fmin(a, eigen_step(b, b.W(W_LXI), b.dX, prm.tau));
+        bt = fmin(bt, eigen_step(b, b.W(W_LSI), b.dS, prm.tau));
+      }
+      if (P.ns > 0) {
+        a = fmin(a, prm.tau * max_scalar_step(P.x, P.delx));
+        bt = fmin(bt, prm.tau * max_scalar_step(P.z, P.delz));
+      }
+    } else {
+      a = backtrack(true);
+      bt = backtrack(false);
+    }
+  }
+
+  // src/step.jl:231-243
+  __device__ double affine_complementarity(double a, double bt) {
+    double s = 0.0;
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      double t = 0.0;
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) {
+        const double x = b.X[k], sv = b.S[k], dx = b.dX[k], ds = b.dS[k];
+        t += x * sv + bt * (x * ds) + a * (dx * sv) + a * bt * (dx * ds);
+      }
+      s += block_sum(t, &sh.rb);
+    }
+    double t = 0.0;
+    for (int k = threadIdx.x; k < P.ns; k += NTHREADS) t += (P.x[k] + a * P.delx[k]) * (P.z[k] + bt * P.delz[k]);
+    s += block_sum(t, &sh.rb);
+    return s / fmax((double)nu(), 1.0);
+  }
+
+  // src/primal_dual.jl:56-72
+  __noinline__ __device__ void take_step(double a, double bt) {
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const int n = b.n;
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) {
+        const int r = (int)(k % n), c = (int)(k / n);
+        if (r > c) {
+          const int64_t kt = c + (int64_t)r * n;
+          const double xv = ((b.X[k] + a * b.dX[k]) + (b.X[kt] + a * b.dX[kt])) / 2;
+          b.X[k] = xv; b.X[kt] = xv;
+          const double sv = ((b.S[k] + bt * b.dS[k]) + (b.S[kt] + bt * b.dS[kt])) / 2;
+          b.S[k] = sv; b.S[kt] = sv;
+        } else if (r == c) {
+          b.X[k] += a * b.dX[k];
+          b.S[k] += bt * b.dS[k];
+        }
+      }
+      __syncthreads();
+    }
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.y[j] += bt * P.dely[j];
+    for (int k = threadIdx.x; k < P.ns; k += NTHREADS) {
+      P.x[k] += a * P.delx[k];
+      P.z[k] += bt * P.delz[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      P.sc[SC_ALPHA] = a;
+      P.sc[SC_BETA] = bt;
+      P.sc[SC_ITER] += 1.0;
+    }
+    __syncthreads();
+    update_residuals();
+  }
+
+  __device__ void solve_directions(double mu, bool corrected) {
+    rhs(mu, corrected);
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.dely[j] = P.h[j];
+    __syncthreads();
+    schur_solve(P.dely);
+    directions(mu, corrected);
+  }
+
+  // One Mehrotra predictor-corrector iteration (src/primal_dual.jl:85-101).
+  // Returns false if it failed before taking a step.
+  __noinline__ __device__ bool iterate_mehrotra(bool strict) {
+    if (!prepare() || !factorize_schur()) return false;
+    const double mu = total_complementarity() / fmax((double)nu(), 1.0);
+    if (threadIdx.x == 0) P.sc[SC_MU] = mu;
+    __syncthreads();
+    solve_directions(0.0, false);
+    double a_aff, b_aff;
+    step_lengths(a_aff, b_aff);
+    const double mu_aff = affine_complementarity(a_aff, b_aff);
+    const double sigma = fmin(fmax(pow(mu_aff / fmax(mu, 2.220446049250313e-16), prm.sigma_exponent), 1e-8), 1.0);
+    if (threadIdx.x == 0) P.sc[SC_SIGMA] = sigma;
+    __syncthreads();
+    correction();
+    solve_directions(sigma * mu, true);
+    double a, bt;
+    step_lengths(a, bt);
+    if (!strict && !(fmin(a, bt) >= 0.2)) return false;
+    take_step(a, bt);
+    return true;
+  }
+
+  // One mc_psd iteration (src/primal_dual.jl:104-121).
+  __noinline__ __device__ bool iterate_adaptive(bool strict) {
+    if (!prepare() || !factorize_schur()) return false;
+    const double mu0 = P.sc[SC_MU];
+    solve_directions(mu0, false);
+    double a, bt;
+    step_lengths(a, bt);
+    if (!strict && !(fmin(a, bt) >= 0.2)) return false;
+    take_step(a, bt);
+    double mu = prm.ratio * total_complementarity() / fmax((double)nu(), 1.0);
+    if (fmin(a, bt) < 0.5) mu *= 1.5;
+    if (a + bt > 1.6) mu *= 0.75;
+    if (a + bt > 1.9) mu /= 1.0 + 0.1 * P.sc[SC_ITER];
+    if (threadIdx.x == 0) P.sc[SC_MU] = mu;
+    __syncthreads();
+    return true;
+  }
+
+  __device__ bool iterate_pd(bool strict) {
+    return prm.centering == MSDP_MEHROTRA ? iterate_mehrotra(strict) : iterate_adaptive(strict);
+  }
+};
+
+template <> __device__ __forceinline__ const double* Algo<double>::xt(const Blk<double>& b) const { return b.X; }
+template <> __device__ __forceinline__ const float* Algo<float>::xt(const Blk<float>& b) const { return b.W(W_XT); }
+template <> __device__ __forceinline__ double* Algo<double>::schur_H() { return P.H64; }
+template <> __device__ __forceinline__ double* Algo<double>::schur_L() { return P.H64; }
+template <> __device__ __forceinline__ float* Algo<float>::schur_H() { return P.Hf; }
+template <> __device__ __forceinline__ float* Algo<float>::schur_L() { return P.Lf; }
+
+template <> __device__ void Algo<double>::schur_solve(double* x) {
+  cta_potrs<double, double>(P.m, P.H64, x);
+}
+
+template <> __device__ void Algo<float>::schur_solve(double* x) {
+  // x0 = L^-T L^-1 h in float; then r = h - H x (float64 accumulation of
+  // the float matrix) and x += solve(r), twice.
+  const int m = P.m;
+  double* h = P.wm;   // original right-hand side
+  double* r = P.wm2;  // residual / correction
+  for (int j = threadIdx.x; j < m; j += NTHREADS) { h[j] = x[j]; r[j] = x[j]; }
+  __syncthreads();
+  cta_potrs<float, double>(m, P.Lf, r);
+  for (int j = threadIdx.x; j < m; j += NTHREADS) x[j] = r[j];
+  __syncthreads();
+  for (int it = 0; it < 2; ++it) {
+    for (int j = threadIdx.x; j < m; j += NTHREADS) {
+      double s = h[j];
+      for (int k = 0; k < m; ++k) s -= (double)P.Hf[j + (int64_t)k * m] * x[k];
+      r[j] = s;
+    }
+    __syncthreads();
+    cta_potrs<float, double>(m, P.Lf, r);
+    for (int j = threadIdx.x; j < m; j += NTHREADS) x[j] += r[j];
+    __syncthreads();
+  }
+}
+
+}  // namespace

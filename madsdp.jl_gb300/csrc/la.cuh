@@ -1,0 +1,411 @@
+// CTA-cooperative dense linear algebra for the per-problem IPM kernel.
+//
+// Every routine is called by all NTHREADS threads of one CTA and ends with a
+// __syncthreads(), so results are visible to the whole CTA on return.
+// Matrices are column-major with leading dimension n (A(i,j) = A[i + j*n]);
+// pointers may address global or shared memory (generic addressing).
+// T is the compute type (double for the FP64 path, float for the FP32
+// phase of the mixed path).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define NTHREADS 256
+#define NWARPS (NTHREADS / 32)
+
+template <class T> struct Num;
+template <> struct Num<double> {
+  static __device__ __forceinline__ double eps() { return 2.220446049250313e-16; }
+  static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+  static __device__ __forceinline__ double rsqrt_(double x) { return rsqrt(x); }
+  static __device__ __forceinline__ bool finite(double x) { return isfinite(x); }
+};
+template <> struct Num<float> {
+  static __device__ __forceinline__ float eps() { return 1.1920928955078125e-7f; }
+  static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+  static __device__ __forceinline__ float rsqrt_(float x) { return rsqrtf(x); }
+  static __device__ __forceinline__ bool finite(float x) { return isfinite(x); }
+};
+
+// ---------------------------------------------------------------- reductions
+template <class T> __device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+template <class T> __device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Scratch for block reductions (NWARPS doubles + result).
+struct RedBuf { double v[NWARPS + 1]; };
+
+__device__ __forceinline__ double block_sum(double v, RedBuf* rb) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) rb->v[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    double r = lane < NWARPS ? rb->v[lane] : 0.0;
+    r = warp_sum(r);
+    if (lane == 0) rb->v[NWARPS] = r;
+  }
+  __syncthreads();
+  double r = rb->v[NWARPS];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_max(double v, RedBuf* rb) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_max(v);
+  if (lane == 0) rb->v[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    double r = lane < NWARPS ? rb->v[lane] : -INFINITY;
+    r = warp_max(r);
+    if (lane == 0) rb->v[NWARPS] = r;
+  }
+  __syncthreads();
+  double r = rb->v[NWARPS];
+  __syncthreads();
+  return r;
+}
+
+// ---------------------------------------------------------------- elementwise
+template <class T, class U>
+__device__ void cta_convert(int64_t len, T* __restrict__ dst, const U* __restrict__ src) {
+  for (int64_t k = threadIdx.x; k < len; k += NTHREADS) dst[k] = (T)src[k];
+  __syncthreads();
+}
+template <class T> __device__ void cta_fill(int64_t len, T* dst, T v) {
+  for (int64_t k = threadIdx.x; k < len; k += NTHREADS) dst[k] = v;
+  __syncthreads();
+}
+// A = (A + A') / 2 in place (src/blocks.jl:77-84).  Each unordered pair is
+// owned by one thread.
+template <class T> __device__ void cta_symmetrize(int n, T* A) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+    int i = (int)(k % n), j = (int)(k / n);
+    if (i > j) {
+      T v = (A[i + (int64_t)j * n] + A[j + (int64_t)i * n]) / (T)2;
+      A[i + (int64_t)j * n] = v;
+      A[j + (int64_t)i * n] = v;
+    }
+  }
+  __syncthreads();
+}
+// dst = sym(src) into another buffer.
+template <class T, class U> __device__ void cta_sym_copy(int n, T* dst, const U* src) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+    int i = (int)(k % n), j = (int)(k / n);
+    dst[k] = (T)((src[i + (int64_t)j * n] + src[j + (int64_t)i * n]) / (U)2);
+  }
+  __syncthreads();
+}
+template <class T> __device__ void cta_set_identity(int n, T* A, T diag) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) A[k] = ((k % n) == (k / n)) ? diag : (T)0;
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- GEMM
+// C = alpha * op(A) * op(B) + beta * C for n x n matrices.  ta/tb: 0 = as
+// stored, 1 = transposed.  loA/loB: the stored operand is lower triangular
+// (its upper triangle is zero), which restricts the k range.  C must not
+// alias A or B.  Each thread owns R x R output micro-tiles.
+template <class T, int R>
+__device__ void cta_gemm_r(int n, int ta, int tb, int loA, int loB, T alpha, const T* __restrict__ A,
+                           const T* __restrict__ B, T beta, T* __restrict__ C) {
+  const int nb = (n + R - 1) / R;
+  const int tiles = nb * nb;
+  for (int t = threadIdx.x; t < tiles; t += NTHREADS) {
+    const int i0 = (t % nb) * R, j0 = (t / nb) * R;
+    int klo = 0, khi = n;  // k in [klo, khi)
+    if (loA) {
+      if (!ta) khi = min(khi, i0 + R);  // A(i,k) != 0 -> k <= i
+      else klo = max(klo, i0);          // A(k,i) != 0 -> k >= i
+    }
+    if (loB) {
+      if (!tb) klo = max(klo, j0);      // B(k,j) != 0 -> k >= j
+      else khi = min(khi, j0 + R);      // B(j,k) != 0 -> k <= j
+    }
+    T acc[R][R];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int c = 0; c < R; ++c) acc[r][c] = (T)0;
+    for (int k = klo; k < khi; ++k) {
+      T a[R], b[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int i = i0 + r;
+        a[r] = (i < n) ? (ta ? A[k + (int64_t)i * n] : A[i + (int64_t)k * n]) : (T)0;
+      }
+#pragma unroll
+      for (int c = 0; c < R; ++c) {
+        const int j = j0 + c;
+        b[c] = (j < n) ? (tb ? B[j + (int64_t)k * n] : B[k + (int64_t)j * n]) : (T)0;
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int c = 0; c < R; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int c = 0; c < R; ++c) {
+        const int i = i0 + r, j = j0 + c;
+        if (i < n && j < n) {
+          const int64_t o = i + (int64_t)j * n;
+          C[o] = (beta == (T)0) ? alpha * acc[r][c] : fma(alpha, acc[r][c], beta * C[o]);
+        }
+      }
+  }
+  __syncthreads();
+}
+
+template <class T>
+__device__ __forceinline__ void cta_gemm(int n, int ta, int tb, int loA, int loB, T alpha, const T* A,
+                                         const T* B, T beta, T* C) {
+  if (n <= 24) cta_gemm_r<T, 2>(n, ta, tb, loA, loB, alpha, A, B, beta, C);
+  else cta_gemm_r<T, 4>(n, ta, tb, loA, loB, alpha, A, B, beta, C);
+}
+
+// ---------------------------------------------------------------- Cholesky
+// In-place lower Cholesky of the n x n matrix `a` (leading dimension lda);
+// only the lower triangle is read.  Returns false (on every thread) if a
+// pivot is not positive and finite, as LAPACK potrf (src/blocks.jl:94-100,
+// src/schur_solvers.jl:15-19).  `flag` is a shared int.
+template <class T>
+__device__ bool cta_potrf(int n, T* a, int lda, int* flag) {
+  if (threadIdx.x == 0) *flag = 0;
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    T* colk = a + (int64_t)k * lda;
+    if (threadIdx.x == 0) {
+      T d = colk[k];
+      if (!(d > (T)0) || !Num<T>::finite(d)) *flag = 1;
+      else colk[k] = Num<T>::sqrt_(d);
+    }
+    __syncthreads();
+    if (*flag) return false;
+    const T inv = (T)1 / colk[k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += NTHREADS) colk[i] *= inv;
+    __syncthreads();
+    const int m = n - k - 1;
+    const int mm = m * m;
+    for (int idx = threadIdx.x; idx < mm; idx += NTHREADS) {
+      const int ii = idx % m, jj = idx / m;
+      if (ii >= jj) {
+        const int i = k + 1 + ii, j = k + 1 + jj;
+        a[i + (int64_t)j * lda] = fma(-colk[i], colk[j], a[i + (int64_t)j * lda]);
+      }
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// Zero the strict upper triangle and flush the entries below
+// eps^2 * max |L_ii| (src/blocks.jl:101-111).  Works on any leading dim.
+template <class T>
+__device__ void cta_flush_lower(int n, T* L, int lda, RedBuf* rb) {
+  double dmax = 0.0;
+  for (int i = threadIdx.x; i < n; i += NTHREADS) dmax = fmax(dmax, fabs((double)L[i + (int64_t)i * lda]));
+  dmax = block_max(dmax, rb);
+  const T tol = (T)((double)Num<T>::eps() * (double)Num<T>::eps() * dmax);
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+    const int i = (int)(k % n), j = (int)(k / n);
+    T* p = L + i + (int64_t)j * lda;
+    if (i < j) *p = (T)0;
+    else if (i > j && fabs(*p) < tol) *p = (T)0;
+  }
+  __syncthreads();
+}
+
+// Inverse of a lower-triangular L (ld = n) into Li (ld = n, lower, upper
+// zeroed).  One thread per column; Li may live in shared memory.
+template <class T>
+__device__ void cta_trtri_lower(int n, const T* __restrict__ L, T* __restrict__ Li) {
+  for (int j = threadIdx.x; j < n; j += NTHREADS) {
+    T* x = Li + (int64_t)j * n;
+    for (int i = 0; i < j; ++i) x[i] = (T)0;
+    x[j] = (T)1 / L[j + (int64_t)j * n];
+    for (int i = j + 1; i < n; ++i) {
+      T s = (T)0;
+      for (int k = j; k < i; ++k) s = fma(L[i + (int64_t)k * n], x[k], s);
+      x[i] = -s / L[i + (int64_t)i * n];
+    }
+  }
+  __syncthreads();
+}
+
+// Solve L L' x = b in place (L lower, ld = n), b of length n.
+template <class T, class V>
+__device__ void cta_potrs(int n, const T* __restrict__ L, V* x) {
+  // forward: L u = b (column oriented)
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) x[k] = x[k] / (V)L[k + (int64_t)k * n];
+    __syncthreads();
+    const V xk = x[k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += NTHREADS) x[i] -= (V)L[i + (int64_t)k * n] * xk;
+    __syncthreads();
+  }
+  // backward: L' x = u (row of L' = column of L: dot products)
+  for (int k = n - 1; k >= 0; --k) {
+    // x[k] = (x[k] - sum_{i>k} L(i,k) x[i]) / L(k,k)
+    V s = 0;
+    for (int i = k + 1 + threadIdx.x; i < n; i += NTHREADS) s += (V)L[i + (int64_t)k * n] * x[i];
+    s = warp_sum(s);
+    __shared__ V part[NWARPS];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      V t = 0;
+      for (int w = 0; w < NWARPS; ++w) t += part[w];
+      x[k] = (x[k] - t) / (V)L[k + (int64_t)k * n];
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------- Jacobi SVD
+// One-sided (Hestenes) Jacobi on the columns of M (n x n, ld n): on return
+// M V has mutually orthogonal columns, V is orthogonal and sigma[k] is the
+// norm of column k of M V.  The eigenvalues of M'M are sigma^2 with
+// eigenvectors V, which is what LowRankOpt.eigen! returns for the NT
+// scaling (src/directions.jl:52-58).  Parallel round-robin ordering, one
+// warp per column pair.  Returns false if it did not converge in max_sweeps.
+template <class T>
+__device__ bool cta_jacobi_svd(int n, T* M, T* V, T* sigma, int max_sweeps, int* counter) {
+  cta_set_identity<T>(n, V, (T)1);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int N = (n % 2 == 0) ? n : n + 1;
+  const T tol = (T)sqrt((double)n) * Num<T>::eps();
+  bool converged = (n <= 1);
+  for (int sweep = 0; sweep < max_sweeps && !converged; ++sweep) {
+    if (threadIdx.x == 0) *counter = 0;
+    __syncthreads();
+    for (int r = 0; r < N - 1; ++r) {
+      for (int k = warp; k < N / 2; k += NWARPS) {
+        int p, q;
+        if (k == 0) { p = N - 1; q = r; }
+        else { p = (r + k) % (N - 1); q = (r - k + (N - 1)) % (N - 1); }
+        if (p >= n || q >= n) continue;
+        T* mp = M + (int64_t)p * n;
+        T* mq = M + (int64_t)q * n;
+        T app = 0, aqq = 0, apq = 0;
+        for (int i = lane; i < n; i += 32) {
+          const T a = mp[i], b = mq[i];
+          app = fma(a, a, app); aqq = fma(b, b, aqq); apq = fma(a, b, apq);
+        }
+        app = warp_sum(app); aqq = warp_sum(aqq); apq = warp_sum(apq);
+        if (!(fabs(apq) > tol * Num<T>::sqrt_(app) * Num<T>::sqrt_(aqq))) continue;
+        const T zeta = (aqq - app) / ((T)2 * apq);
+        const T t = (zeta >= (T)0 ? (T)1 : (T)-1) / (fabs(zeta) + Num<T>::sqrt_((T)1 + zeta * zeta));
+        const T c = Num<T>::rsqrt_((T)1 + t * t), s = c * t;
+        for (int i = lane; i < n; i += 32) {
+          const T a = mp[i], b = mq[i];
+          mp[i] = c * a - s * b;
+          mq[i] = s * a + c * b;
+        }
+        T* vp = V + (int64_t)p * n;
+        T* vq = V + (int64_t)q * n;
+        for (int i = lane; i < n; i += 32) {
+          const T a = vp[i], b = vq[i];
+          vp[i] = c * a - s * b;
+          vq[i] = s * a + c * b;
+        }
+        if (lane == 0) atomicAdd(counter, 1);
+      }
+      __syncthreads();
+    }
+    converged = (*counter == 0);
+    __syncthreads();
+  }
+  // column norms
+  for (int k = warp; k < n; k += NWARPS) {
+    const T* mk = M + (int64_t)k * n;
+    T s = 0;
+    for (int i = lane; i < n; i += 32) s = fma(mk[i], mk[i], s);
+    s = warp_sum(s);
+    if (lane == 0) sigma[k] = Num<T>::sqrt_(s);
+  }
+  __syncthreads();
+  return converged;
+}
+
+// ---------------------------------------------------------------- tridiagonal
+// Number of eigenvalues of the symmetric tridiagonal (a[0..k), b[1..k))
+// smaller than x (Sturm count).
+template <class T>
+__device__ __forceinline__ int sturm_count(int k, const T* a, const T* b, T x, T pivmin) {
+  int cnt = 0;
+  T d = a[0] - x;
+  if (fabs(d) < pivmin) d = -pivmin;
+  if (d < 0) ++cnt;
+  for (int i = 1; i < k; ++i) {
+    d = (a[i] - x) - b[i] * b[i] / d;
+    if (fabs(d) < pivmin) d = -pivmin;
+    if (d < 0) ++cnt;
+  }
+  return cnt;
+}
+
+// Smallest eigenvalue of the tridiagonal (a, b) by warp-parallel multisection.
+// Called by one full warp; every lane returns the result.
+template <class T>
+__device__ T warp_tridiag_eigmin(int k, const T* a, const T* b) {
+  const int lane = threadIdx.x & 31;
+  T lo = 0, hi = 0, scale = 0;
+  // Gershgorin interval
+  for (int i = 0; i < k; ++i) {
+    const T r = (i > 0 ? fabs(b[i]) : (T)0) + (i + 1 < k ? fabs(b[i + 1]) : (T)0);
+    const T l = a[i] - r, h = a[i] + r;
+    if (i == 0 || l < lo) lo = l;
+    if (i == 0 || h > hi) hi = h;
+    scale = fmax(scale, fmax(fabs(l), fabs(h)));
+  }
+  const T pivmin = (T)(Num<T>::eps() * Num<T>::eps()) * fmax(scale, (T)1e-30);
+  for (int it = 0; it < 64; ++it) {
+    if (hi - lo <= (T)2 * Num<T>::eps() * fmax(fabs(lo), fabs(hi)) + pivmin) break;
+    const T x = lo + (hi - lo) * (T)(lane + 1) / (T)33;
+    const int c = sturm_count(k, a, b, x, pivmin);
+    const unsigned ball = __ballot_sync(0xffffffffu, c >= 1);
+    if (ball == 0) { lo = lo + (hi - lo) * (T)32 / (T)33; continue; }
+    const int first = __ffs(ball) - 1;  // smallest lane with count >= 1
+    const T nhi = lo + (hi - lo) * (T)(first + 1) / (T)33;
+    const T nlo = first == 0 ? lo : lo + (hi - lo) * (T)first / (T)33;
+    lo = nlo; hi = nhi;
+  }
+  return (lo + hi) / (T)2;
+}
+
+// The j-th smallest eigenvalue (0-based) of the tridiagonal by bisection,
+// computed by one thread.
+template <class T>
+__device__ T thread_tridiag_eig(int k, const T* a, const T* b, int j) {
+  T lo = 0, hi = 0, scale = 0;
+  for (int i = 0; i < k; ++i) {
+    const T r = (i > 0 ? fabs(b[i]) : (T)0) + (i + 1 < k ? fabs(b[i + 1]) : (T)0);
+    const T l = a[i] - r, h = a[i] + r;
+    if (i == 0 || l < lo) lo = l;
+    if (i == 0 || h > hi) hi = h;
+    scale = fmax(scale, fmax(fabs(l), fabs(h)));
+  }
+  const T pivmin = (T)(Num<T>::eps() * Num<T>::eps()) * fmax(scale, (T)1e-30);
+  for (int it = 0; it < 200; ++it) {
+    if (hi - lo <= (T)2 * Num<T>::eps() * fmax(fabs(lo), fabs(hi)) + pivmin) break;
+    const T x = (lo + hi) / (T)2;
+    if (sturm_count(k, a, b, x, pivmin) >= j + 1) hi = x;
+    else lo = x;
+  }
+  return (lo + hi) / (T)2;
+}

@@ -1,0 +1,422 @@
+"""Host-side mirror of MadSDP's solver API over the C ABI.
+
+``MadSDPSolver(model; components..., options...)`` / ``solve()`` /
+``madsdp(model)`` follow src/solver.jl:55-160,385-404; ``Batch`` solves
+many models in one persistent launch (one CTA per problem at a time).
+Errors follow the reference: invalid configurations raise ``ValueError``
+(Julia ``ArgumentError``), an impossible initial point raises
+``RuntimeError`` (Julia ``ErrorException``).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .components import (AdaptiveMu, CholeskyBacktrack, DenseCholesky, DualCentering, DualShift,
+                         EigenStep, HKM, InitialPoint, MadNLPSchur, Mehrotra, NT, Options,
+                         PRECISIONS, PrimalDual, QRSchur, ScaledIdentity, Status)
+from .model import Model
+
+__all__ = ["Context", "Batch", "MadSDPSolver", "madsdp", "GPUError", "default_context"]
+
+P = C.POINTER
+f64p = P(C.c_double)
+
+
+class GPUError(RuntimeError):
+    """A CUDA or library error reported through the C ABI."""
+
+
+_default_ctx = None
+
+
+class Context:
+    """One CUDA device and one stream (msdp_context)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        rc = self.lib.msdp_context_create(device, C.byref(h))
+        if rc != 0:
+            raise GPUError(f"msdp_context_create failed ({_lib.ERRORS.get(rc, rc)})")
+        self.h = h
+        self.device = device
+
+    def error(self) -> str:
+        return self.lib.msdp_last_error(self.h).decode()
+
+    def check(self, rc: int, what: str):
+        if rc == 0:
+            return
+        msg = self.error()
+        if rc == -1:
+            raise ValueError(msg)
+        if rc == -5:
+            raise RuntimeError(msg)
+        if rc == -4:
+            raise NotImplementedError(msg)
+        raise GPUError(f"{what}: {_lib.ERRORS.get(rc, rc)}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.msdp_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _ptr(a: np.ndarray, ctype=C.c_double):
+    return a.ctypes.data_as(P(ctype))
+
+
+def _components(algorithm, initial_point, schur, precision) -> _lib.Components:
+    c = _lib.Components()
+    _lib.load().msdp_default_components(C.byref(c))
+    if isinstance(algorithm, DualCentering):
+        c.algorithm = 1
+        c.dc_beta, c.dc_delta = algorithm.beta, algorithm.delta
+        c.dc_A = math.nan if algorithm.A is None else float(algorithm.A)
+        c.centering_max_iter = algorithm.centering_max_iter
+    else:
+        c.algorithm = 0
+        d, s, ce = algorithm.direction, algorithm.step, algorithm.centering
+        c.direction = d.code
+        c.step = s.code
+        if isinstance(s, EigenStep):
+            c.tau = s.tau
+        else:
+            c.shrink, c.boundary = s.shrink, s.boundary
+        c.centering = ce.code
+        if isinstance(ce, Mehrotra):
+            c.sigma_exponent = ce.sigma_exponent
+        else:
+            c.initial_ratio, c.ratio = ce.initial_ratio, ce.ratio
+    c.initial_point = initial_point.code
+    if isinstance(initial_point, ScaledIdentity):
+        c.scale = 0.0 if initial_point.scale is None else initial_point.scale
+    elif isinstance(initial_point, DualShift):
+        c.initial_shift, c.max_shift = initial_point.initial_shift, initial_point.max_shift
+    c.schur = schur.code
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+    c.precision = PRECISIONS[precision]
+    return c
+
+
+def _options(opt: Options) -> _lib.Options:
+    o = _lib.Options()
+    _lib.load().msdp_default_options(C.byref(o))
+    o.tol, o.max_iter, o.max_wall_time = opt.tol, opt.max_iter, opt.max_wall_time
+    o.mu_min, o.regularize_schur, o.max_schur_reg = opt.mu_min, opt.regularize_schur, opt.max_schur_reg
+    o.datasparsity, o.switch_tol = opt.datasparsity, opt.switch_tol
+    return o
+
+
+class _Marshalled:
+    """Keeps the numpy buffers of one problem alive while the C call runs."""
+
+    def __init__(self, model: Model):
+        nb = model.nblocks
+        self.sides = np.array(model.sides, dtype=np.int32)
+        self.C = [np.asfortranarray(c, dtype=np.float64) for c in model.C]
+        self.nnz = np.array([a.nnz for a in model.A], dtype=np.int64)
+        self.con = [np.ascontiguousarray(a.con, dtype=np.int32) for a in model.A]
+        self.row = [np.ascontiguousarray(a.row, dtype=np.int32) for a in model.A]
+        self.col = [np.ascontiguousarray(a.col, dtype=np.int32) for a in model.A]
+        self.val = [np.ascontiguousarray(a.val, dtype=np.float64) for a in model.A]
+        self.b = np.ascontiguousarray(model.b, dtype=np.float64)
+        self.d = np.ascontiguousarray(model.d_lin, dtype=np.float64)
+        self.Cl = np.asfortranarray(model.C_lin, dtype=np.float64)
+        self.Cp = (f64p * max(nb, 1))(*[_ptr(c) for c in self.C])
+        self.conp = (P(C.c_int32) * max(nb, 1))(*[_ptr(a, C.c_int32) for a in self.con])
+        self.rowp = (P(C.c_int32) * max(nb, 1))(*[_ptr(a, C.c_int32) for a in self.row])
+        self.colp = (P(C.c_int32) * max(nb, 1))(*[_ptr(a, C.c_int32) for a in self.col])
+        self.valp = (f64p * max(nb, 1))(*[_ptr(a) for a in self.val])
+        d = _lib.ProblemDesc()
+        d.nblocks, d.m, d.ns = nb, model.m, model.ns
+        d.sides = _ptr(self.sides, C.c_int32)
+        d.C = self.Cp
+        d.A_nnz = _ptr(self.nnz, C.c_int64)
+        d.A_con, d.A_row, d.A_col, d.A_val = self.conp, self.rowp, self.colp, self.valp
+        d.b, d.d_lin, d.C_lin = _ptr(self.b), _ptr(self.d), _ptr(self.Cl)
+        self.desc = d
+
+
+class Batch:
+    """Many problems resident on one GPU, solved by one persistent launch."""
+
+    def __init__(self, models: Sequence[Model], algorithm=None, direction=None, step=None,
+                 centering=None, initial_point=None, schur=None, precision: str = "fp64",
+                 context: Optional[Context] = None, **options):
+        self.ctx = context or default_context()
+        self.lib = self.ctx.lib
+        direction = NT() if direction is None else direction
+        step = EigenStep() if step is None else step
+        centering = Mehrotra() if centering is None else centering
+        self.algorithm = PrimalDual(direction, step, centering) if algorithm is None else algorithm
+        if initial_point is None:
+            initial_point = DualShift() if isinstance(self.algorithm, DualCentering) else ScaledIdentity()
+        self.initial_point = initial_point
+        self.schur = DenseCholesky() if schur is None else schur
+        self.precision = precision
+        self.opt = Options(**options)
+        self.models = list(models)
+        if not self.models:
+            raise ValueError("a batch needs at least one model")
+        if isinstance(self.schur, QRSchur):
+            if not (isinstance(self.algorithm, PrimalDual) and isinstance(self.algorithm.direction, NT)):
+                raise ValueError("QRSchur requires PrimalDual with the NT direction.")
+        if isinstance(self.algorithm, DualCentering):
+            for m in self.models:
+                if m.ns > 0:
+                    raise RuntimeError("MadSDP: `DualCentering` does not support scalar (LP) blocks yet.")
+                if m.nblocks == 0:
+                    raise RuntimeError("MadSDP: `DualCentering` needs at least one PSD block.")
+        marsh = [_Marshalled(m) for m in self.models]
+        descs = (_lib.ProblemDesc * len(marsh))(*[mm.desc for mm in marsh])
+        comp = _components(self.algorithm, self.initial_point, self.schur, precision)
+        opts = _options(self.opt)
+        h = C.c_void_p()
+        rc = self.lib.msdp_batch_create(self.ctx.h, descs, len(marsh), C.byref(comp), C.byref(opts), C.byref(h))
+        self.ctx.check(rc, "msdp_batch_create")
+        self.h = h
+        self.nprob = len(marsh)
+        if isinstance(self.initial_point, InitialPoint):
+            for p in range(self.nprob):
+                self.set_initial_point(p, self.initial_point)
+
+    # --- lifecycle -------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.msdp_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.lib.msdp_batch_device_bytes(self.h))
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.msdp_batch_launch_count(self.h))
+
+    def set_initial_point(self, p: int, ip: InitialPoint):
+        m = self.models[p]
+        Xs = [np.asfortranarray(x, dtype=np.float64) for x in ip.X]
+        Xp = (f64p * max(len(Xs), 1))(*[_ptr(x) for x in Xs])
+        y = np.ascontiguousarray(ip.y, dtype=np.float64)
+        x = None if ip.x is None else np.ascontiguousarray(ip.x, dtype=np.float64)
+        rc = self.lib.msdp_batch_set_initial_point(self.h, p, Xp, _ptr(y), None if x is None else _ptr(x))
+        self.ctx.check(rc, "msdp_batch_set_initial_point")
+
+    def set_iterate(self, p: int, X=None, S=None, y=None, x=None, z=None):
+        nb = self.models[p].nblocks
+        keep = []
+
+        def mats(Ms):
+            if Ms is None:
+                return None
+            arrs = [np.asfortranarray(a, dtype=np.float64) for a in Ms]
+            keep.append(arrs)
+            return (f64p * max(nb, 1))(*[_ptr(a) for a in arrs])
+
+        def vec(v):
+            if v is None:
+                return None
+            a = np.ascontiguousarray(v, dtype=np.float64)
+            keep.append(a)
+            return _ptr(a)
+
+        rc = self.lib.msdp_batch_set_iterate(self.h, p, mats(X), mats(S), vec(y), vec(x), vec(z))
+        self.ctx.check(rc, "msdp_batch_set_iterate")
+
+    def initialize(self):
+        self.ctx.check(self.lib.msdp_batch_initialize(self.h), "msdp_batch_initialize")
+
+    def iterate(self, max_iterations: int = 0, sync: bool = True):
+        self.ctx.check(self.lib.msdp_batch_iterate(self.h, max_iterations), "msdp_batch_iterate")
+        if sync:
+            self.synchronize()
+
+    def synchronize(self):
+        self.ctx.check(self.lib.msdp_batch_synchronize(self.h), "msdp_batch_synchronize")
+
+    def solve(self):
+        self.ctx.check(self.lib.msdp_batch_solve(self.h), "msdp_batch_solve")
+        return self
+
+    # --- results -----------------------------------------------------------------
+    def stats(self, p: int) -> dict:
+        s = _lib.Stats()
+        self.ctx.check(self.lib.msdp_batch_get_stats(self.h, p, C.byref(s)), "msdp_batch_get_stats")
+        return _stats_dict(s)
+
+    def all_stats(self) -> List[dict]:
+        arr = (_lib.Stats * self.nprob)()
+        self.ctx.check(self.lib.msdp_batch_get_all_stats(self.h, arr), "msdp_batch_get_all_stats")
+        return [_stats_dict(s) for s in arr]
+
+    def solution(self, p: int):
+        m = self.models[p]
+        X = [np.zeros((n, n), order="F") for n in m.sides]
+        Xp = (f64p * max(len(X), 1))(*[_ptr(a) for a in X])
+        y, x, z = np.zeros(m.m), np.zeros(m.ns), np.zeros(m.ns)
+        rc = self.lib.msdp_batch_get_solution(self.h, p, Xp, _ptr(y), _ptr(x), _ptr(z))
+        self.ctx.check(rc, "msdp_batch_get_solution")
+        return [np.ascontiguousarray(a) for a in X], y, x, z
+
+    def trajectory(self, p: int) -> List[dict]:
+        cap = self.opt.max_iter + 2
+        arr = (_lib.IterRecord * cap)()
+        cnt = C.c_int32()
+        rc = self.lib.msdp_batch_get_trajectory(self.h, p, arr, cap, C.byref(cnt))
+        self.ctx.check(rc, "msdp_batch_get_trajectory")
+        return [{k: getattr(arr[i], k) for k, _ in _lib.IterRecord._fields_} for i in range(min(cnt.value, cap))]
+
+    # --- component-granular steps (identity tests) -------------------------------
+    def update_residuals(self):
+        self.ctx.check(self.lib.msdp_batch_update_residuals(self.h), "msdp_batch_update_residuals")
+
+    def prepare(self) -> np.ndarray:
+        ok = np.zeros(self.nprob, dtype=np.int32)
+        self.ctx.check(self.lib.msdp_batch_prepare(self.h, _ptr(ok, C.c_int32)), "msdp_batch_prepare")
+        return ok.astype(bool)
+
+    def solve_directions(self, mu: float, corrected: bool):
+        self.ctx.check(self.lib.msdp_batch_solve_directions(self.h, float(mu), int(bool(corrected))),
+                       "msdp_batch_solve_directions")
+
+    def correction(self):
+        self.ctx.check(self.lib.msdp_batch_correction(self.h), "msdp_batch_correction")
+
+    def directions(self, p: int):
+        m = self.models[p]
+        dX = [np.zeros((n, n), order="F") for n in m.sides]
+        dS = [np.zeros((n, n), order="F") for n in m.sides]
+        dXp = (f64p * max(len(dX), 1))(*[_ptr(a) for a in dX])
+        dSp = (f64p * max(len(dS), 1))(*[_ptr(a) for a in dS])
+        dy, dx, dz = np.zeros(m.m), np.zeros(m.ns), np.zeros(m.ns)
+        rc = self.lib.msdp_batch_get_directions(self.h, p, dXp, dSp, _ptr(dy), _ptr(dx), _ptr(dz))
+        self.ctx.check(rc, "msdp_batch_get_directions")
+        return [np.ascontiguousarray(a) for a in dX], [np.ascontiguousarray(a) for a in dS], dy, dx, dz
+
+    def residuals(self, p: int):
+        m = self.models[p]
+        Rd = [np.zeros((n, n), order="F") for n in m.sides]
+        Rdp = (f64p * max(len(Rd), 1))(*[_ptr(a) for a in Rd])
+        Rp, Rdl = np.zeros(m.m), np.zeros(m.ns)
+        rc = self.lib.msdp_batch_get_residuals(self.h, p, _ptr(Rp), Rdp, _ptr(Rdl))
+        self.ctx.check(rc, "msdp_batch_get_residuals")
+        return Rp, [np.ascontiguousarray(a) for a in Rd], Rdl
+
+    def block_matrix(self, p: int, block: int, which: str) -> np.ndarray:
+        code = {"W": 0, "corr": 1, "Si": 2, "S": 3, "X": 4}[which]
+        n = self.models[p].sides[block]
+        out = np.zeros((n, n), order="F")
+        rc = self.lib.msdp_batch_get_block_matrix(self.h, p, block, code, _ptr(out))
+        self.ctx.check(rc, "msdp_batch_get_block_matrix")
+        return np.ascontiguousarray(out)
+
+
+def _stats_dict(s) -> dict:
+    d = {k: getattr(s, k) for k, _ in _lib.Stats._fields_}
+    d["status"] = Status(d["status"]) if d["status"] in Status._value2member_map_ else d["status"]
+    return d
+
+
+class MadSDPSolver:
+    """One problem on the GPU with the constructor of src/solver.jl:87-160."""
+
+    def __init__(self, model: Model, **kwargs):
+        self.model = model
+        self.batch = Batch([model], **kwargs)
+        self._stats = None
+
+    def initialize(self):
+        self.batch.initialize()
+        self._stats = None
+
+    def solve(self, verbose: bool = False):
+        """solve!(solver) (src/solver.jl:385-396)."""
+        self.batch.solve()
+        self._stats = self.batch.stats(0)
+        if verbose:
+            print_trajectory(self.batch.trajectory(0))
+        return self
+
+    def iterate(self, k: int = 1):
+        self.batch.iterate(k)
+        self._stats = None
+
+    @property
+    def stats(self) -> dict:
+        if self._stats is None:
+            self._stats = self.batch.stats(0)
+        return self._stats
+
+    @property
+    def status(self) -> Status:
+        return self.stats["status"]
+
+    @property
+    def iter(self) -> int:
+        return self.stats["iter"]
+
+    def primal_objective(self) -> float:
+        return self.stats["pobj"]
+
+    def dual_objective(self) -> float:
+        return self.stats["dobj"]
+
+    @property
+    def inf_pr(self):
+        return self.stats["inf_pr"]
+
+    @property
+    def inf_du(self):
+        return self.stats["inf_du"]
+
+    @property
+    def inf_compl(self):
+        return self.stats["gap"]
+
+    def solution(self):
+        return self.batch.solution(0)
+
+    def trajectory(self):
+        return self.batch.trajectory(0)
+
+
+def print_trajectory(traj):
+    """The iteration table of src/solver.jl:353-383."""
+    for r in traj:
+        if int(r["iter"]) % 10 == 0:
+            print("%4s %14s %14s %9s %9s %9s %9s %9s" % ("iter", "p_obj", "d_obj", "inf_pr", "inf_du", "gap", "mu", "α/β"))
+        print("%4d %14.6e %14.6e %9.2e %9.2e %9.2e %9.2e %4.2f/%4.2f" % (
+            r["iter"], r["pobj"], r["dobj"], r["inf_pr"], r["inf_du"], r["gap"], r["mu"], r["alpha"], r["beta"]))
+
+
+def madsdp(model: Model, **kwargs) -> MadSDPSolver:
+    """madsdp(model; kwargs...) (src/solver.jl:404)."""
+    return MadSDPSolver(model, **kwargs).solve()
