@@ -147,6 +147,8 @@ void msdp_default_options(msdp_options* o);
 int msdp_context_create(int device, msdp_context** ctx);
 int msdp_context_destroy(msdp_context* ctx);
 const char* msdp_last_error(const msdp_context* ctx);
+/* The cudaStream_t of the context (to time or order work against it). */
+void* msdp_context_stream(const msdp_context* ctx);
 int msdp_device_count(void);
 
 /* A batch of problems solved together (one CTA per problem at a time).
@@ -166,6 +168,13 @@ int msdp_batch_set_iterate(msdp_batch* batch, int32_t prob, const double* const*
                            const double* const* S, const double* y, const double* x, const double* z);
 
 int msdp_batch_initialize(msdp_batch* batch);
+/* Enqueue initialize + iterate-to-termination on the context stream without
+ * waiting (an initial-point failure shows as status 200 in the stats). */
+int msdp_batch_launch_solve(msdp_batch* batch);
+/* Enqueue initialize! only, without waiting. */
+int msdp_batch_launch_initialize(msdp_batch* batch);
+/* Bytes copied host -> device when the batch was created. */
+int64_t msdp_batch_upload_bytes(const msdp_batch* batch);
 /* Run up to `max_iterations` iterations (<= 0: until every problem stops). */
 int msdp_batch_iterate(msdp_batch* batch, int32_t max_iterations);
 int msdp_batch_solve(msdp_batch* batch);

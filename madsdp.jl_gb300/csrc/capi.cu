@@ -42,6 +42,7 @@ struct msdp_batch {
   int64_t n_dd = 0, n_d64 = 0, n_d32 = 0, n_ent = 0, n_ptr = 0;
   int64_t bytes = 0;
   int64_t launches = 0;
+  int64_t upload_bytes = 0;
   int grid = 0;
 };
 
@@ -144,6 +145,8 @@ int msdp_context_destroy(msdp_context* ctx) {
 }
 
 const char* msdp_last_error(const msdp_context* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+void* msdp_context_stream(const msdp_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
 int msdp_batch_destroy(msdp_batch* b) {
   if (!b) return MSDP_OK;
@@ -354,6 +357,9 @@ int msdp_batch_create(msdp_context* ctx, const msdp_problem_desc* probs, int32_t
   up(b->eval, heval.data(), sizeof(double) * o_ent);
   up(b->pval, hpval.data(), sizeof(double) * o_ent);
   up(b->ptr, hptr.data(), sizeof(int64_t) * o_ptr);
+  b->upload_bytes = (int64_t)(sizeof(ProbDesc) * nprob + sizeof(BlockDesc) * nblk_total + sizeof(int32_t) * nprob +
+                              sizeof(double) * o_dd + (3 * sizeof(int32_t) + 2 * sizeof(double)) * o_ent +
+                              sizeof(int64_t) * o_ptr);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d64, 0, sizeof(double) * std::max<int64_t>(o64, 1), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d32, 0, sizeof(float) * std::max<int64_t>(o32, 1), st);
   // staging buffers are pageable: wait before they go out of scope
@@ -507,6 +513,19 @@ int msdp_batch_initialize(msdp_batch* b) {
                   "MadSDP: could not find a dual interior point `y = -rho 1` with rho <= max_shift; "
                   "use `InitialPoint` to give one.");
   return MSDP_OK;
+}
+
+int msdp_batch_launch_initialize(msdp_batch* b) {
+  if (!b) return MSDP_ERR_INVALID_ARGUMENT;
+  return launch(b, OP_INITIALIZE, 0, 0.0, 0);
+}
+
+int64_t msdp_batch_upload_bytes(const msdp_batch* b) { return b ? b->upload_bytes : 0; }
+
+int msdp_batch_launch_solve(msdp_batch* b) {
+  if (!b) return MSDP_ERR_INVALID_ARGUMENT;
+  int rc = launch(b, OP_INITIALIZE, 0, 0.0, 0);
+  return rc ? rc : launch(b, OP_ITERATE, 0, 0.0, 0);
 }
 
 int msdp_batch_iterate(msdp_batch* b, int32_t max_iterations) {

@@ -64,6 +64,7 @@ SIGNATURES = [
     ("msdp_context_create", i32, [C.c_int, P(C.c_void_p)]),
     ("msdp_context_destroy", i32, [C.c_void_p]),
     ("msdp_last_error", C.c_char_p, [C.c_void_p]),
+    ("msdp_context_stream", C.c_void_p, [C.c_void_p]),
     ("msdp_device_count", i32, []),
     ("msdp_batch_create", i32, [C.c_void_p, P(ProblemDesc), i32, P(Components), P(Options), P(C.c_void_p)]),
     ("msdp_batch_destroy", i32, [C.c_void_p]),
@@ -71,6 +72,9 @@ SIGNATURES = [
     ("msdp_batch_set_initial_point", i32, [C.c_void_p, i32, P(P(f64)), P(f64), P(f64)]),
     ("msdp_batch_set_iterate", i32, [C.c_void_p, i32, P(P(f64)), P(P(f64)), P(f64), P(f64), P(f64)]),
     ("msdp_batch_initialize", i32, [C.c_void_p]),
+    ("msdp_batch_launch_solve", i32, [C.c_void_p]),
+    ("msdp_batch_launch_initialize", i32, [C.c_void_p]),
+    ("msdp_batch_upload_bytes", i64, [C.c_void_p]),
     ("msdp_batch_iterate", i32, [C.c_void_p, i32]),
     ("msdp_batch_solve", i32, [C.c_void_p]),
     ("msdp_batch_synchronize", i32, [C.c_void_p]),

@@ -47,6 +47,11 @@ class Context:
         self.h = h
         self.device = device
 
+    @property
+    def stream_handle(self) -> int:
+        """The cudaStream_t of this context as an integer."""
+        return int(self.lib.msdp_context_stream(self.h) or 0)
+
     def error(self) -> str:
         return self.lib.msdp_last_error(self.h).decode()
 
@@ -265,6 +270,18 @@ class Batch:
     def solve(self):
         self.ctx.check(self.lib.msdp_batch_solve(self.h), "msdp_batch_solve")
         return self
+
+    def launch_initialize(self):
+        """Enqueue initialize! on the context stream; returns at once."""
+        self.ctx.check(self.lib.msdp_batch_launch_initialize(self.h), "msdp_batch_launch_initialize")
+
+    @property
+    def upload_bytes(self) -> int:
+        return int(self.lib.msdp_batch_upload_bytes(self.h))
+
+    def launch_solve(self):
+        """Enqueue initialize + solve on the context stream; returns at once."""
+        self.ctx.check(self.lib.msdp_batch_launch_solve(self.h), "msdp_batch_launch_solve")
 
     # --- results -----------------------------------------------------------------
     def stats(self, p: int) -> dict:
