@@ -204,6 +204,12 @@ int msdp_batch_get_block_matrix(msdp_batch* batch, int32_t prob, int32_t block, 
 enum msdp_block_matrix { MSDP_MAT_W = 0, MSDP_MAT_CORR = 1, MSDP_MAT_SI = 2, MSDP_MAT_S = 3,
                          MSDP_MAT_X = 4 };
 
+/* Device profile of problem `prob`: cycle counters per phase and work
+ * counters of the last solve (names in the same order as
+ * msdp_profile_field_name); returns the number of fields written. */
+int msdp_batch_get_profile(msdp_batch* batch, int32_t prob, double* out, int32_t capacity);
+const char* msdp_profile_field_name(int32_t index);
+
 /* Number of kernel launches issued by this batch since creation. */
 int64_t msdp_batch_launch_count(const msdp_batch* batch);
 

@@ -308,6 +308,20 @@ int msdp_batch_create(msdp_context* ctx, const msdp_problem_desc* probs, int32_t
         cptr[con[s] + 1] += 1;
       }
       for (int64_t j = 0; j < m; ++j) cptr[j + 1] += cptr[j];
+      // Hankel 0/1 structure: m = 2n-1 and constraint j holds exactly the
+      // entries (a, j-a) with value 1
+      bool hankel = (m == 2 * n - 1) && nnz == n * n;
+      for (int64_t j = 0; hankel && j < m; ++j) {
+        const int64_t lo = std::max<int64_t>(0, j - n + 1), hi = std::min<int64_t>(j, n - 1);
+        if (cptr[j + 1] - cptr[j] != hi - lo + 1) { hankel = false; break; }
+        int64_t prev_col = -1;
+        for (int64_t q = cptr[j]; q < cptr[j + 1]; ++q) {
+          const int64_t e = bd.ent + q;
+          if (herow[e] + hecol[e] != j || heval[e] != 1.0 || hecol[e] <= prev_col) { hankel = false; break; }
+          prev_col = hecol[e];
+        }
+      }
+      bd.structure = hankel ? STRUCT_HANKEL : STRUCT_GENERAL;
       // by position (counting sort, stable in constraint order)
       int64_t* pptr = hptr.data() + bd.posptr;
       for (int64_t e = 0; e < nnz; ++e) pptr[row[e] + col[e] * n + 1] += 1;
@@ -652,6 +666,34 @@ int msdp_batch_get_residuals(msdp_batch* b, int32_t p, double* Rp, double* const
   if ((rc = copy_d2h(b, Rp, vec64(b, p, V_RP), sizeof(double) * d.m))) return rc;
   if ((rc = copy_d2h(b, Rd_lin, svec64(b, p, S_RDLIN), sizeof(double) * d.ns))) return rc;
   return MSDP_OK;
+}
+
+static const char* kProfileNames[] = {
+    "cycles_cholesky", "cycles_triangular_inverse", "cycles_jacobi", "cycles_nt_products", "cycles_schur_assembly",
+    "cycles_schur_factor", "cycles_rhs", "cycles_schur_solve", "cycles_directions", "cycles_step_length",
+    "cycles_lanczos", "cycles_correction", "cycles_take_step", "cycles_termination", "cycles_iteration",
+    "jacobi_sweeps", "jacobi_calls", "lanczos_steps", "lanczos_calls", "schur_factorizations"};
+
+static std::string g_profile_names[2 * SC_PROFILE_N];
+
+const char* msdp_profile_field_name(int32_t i) {
+  if (i < 0 || i >= 2 * SC_PROFILE_N) return nullptr;
+  if (g_profile_names[i].empty())
+    g_profile_names[i] = std::string(i < SC_PROFILE_N ? "fp32." : "fp64.") + kProfileNames[i % SC_PROFILE_N];
+  return g_profile_names[i].c_str();
+}
+
+int msdp_batch_get_profile(msdp_batch* b, int32_t p, double* out, int32_t capacity) {
+  if (bad_prob(b, p) || !out) return MSDP_ERR_INVALID_ARGUMENT;
+  const int n = std::min<int>(capacity, 2 * SC_PROFILE_N);
+  const ProbDesc& d = b->hprob[p];
+  std::vector<double> sc(SC_COUNT);
+  int rc = copy_d2h(b, sc.data(), b->d64 + d.v64 + (int64_t)V_MCOUNT * d.m + (int64_t)S_COUNT * d.ns,
+                    sizeof(double) * SC_COUNT);
+  if (rc) return rc;
+  for (int k = 0; k < n; ++k)
+    out[k] = sc[SC_T_CHOL + (k % SC_PROFILE_N) + (k < SC_PROFILE_N ? 0 : SC_PROFILE_F64)];
+  return n;
 }
 
 int msdp_batch_get_block_matrix(msdp_batch* b, int32_t p, int32_t block, int32_t which, double* out) {

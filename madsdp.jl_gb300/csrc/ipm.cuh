@@ -16,7 +16,7 @@
 #include "layout.h"
 
 #ifndef MSDP_SMEM_BYTES
-#define MSDP_SMEM_BYTES (200 * 1024)
+#define MSDP_SMEM_BYTES (72 * 1024)
 #endif
 
 // Device code of one translation unit: internal linkage.
@@ -36,6 +36,18 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
+
+// Per-phase device cycle counters (thread 0 accumulates into the scalars).
+#define PROF_BEGIN(tag) const long long prof_##tag = clock64()
+#define PROF_SHIFT (sizeof(T) == 8 ? SC_PROFILE_F64 : 0)
+#define PROF_END(tag, slot)                                                         \
+  do {                                                                              \
+    if (threadIdx.x == 0) P.sc[(slot) + PROF_SHIFT] += (double)(clock64() - prof_##tag); \
+  } while (0)
+#define PROF_COUNT(slot, v)                                                         \
+  do {                                                                              \
+    if (threadIdx.x == 0) P.sc[(slot) + PROF_SHIFT] += (double)(v);                 \
+  } while (0)
 
 // ------------------------------------------------------------------ views
 struct Prob {
@@ -91,6 +103,8 @@ struct Blk {
   const double *eval, *pval;
   const int64_t *cptr, *pptr;
   double cnorm;
+  int structure;
+  int index;
   __device__ __forceinline__ T* W(int k) const { return w + (int64_t)k * nn; }
   __device__ __forceinline__ T* V(int k) const { return w + (int64_t)W_COUNT * nn + (int64_t)k * (n + 1); }
   __device__ __forceinline__ double* M(int k) const { return base + (int64_t)k * nn; }
@@ -116,6 +130,8 @@ __device__ __forceinline__ Blk<T> make_blk(const BatchDev& B, const Prob& P, int
   b.pcon = B.p_con + d.ent; b.pval = B.p_val + d.ent;
   b.cptr = B.ptr + d.conptr; b.pptr = B.ptr + d.posptr;
   b.cnorm = d.cnorm;
+  b.structure = d.structure;
+  b.index = i;
   return b;
 }
 
@@ -234,7 +250,7 @@ __device__ void tri_inverse(int n, const T* L, T* Li, unsigned char* smem) {
 // vectors of length n+1.  Stops when the smallest Ritz value is stable or
 // the Krylov space is exhausted.
 template <class T>
-__device__ T lanczos_eigmin(int n, const T* Z, T* Q, T* a, T* bb, T* w, T* coef, SharedState& sh) {
+__device__ T lanczos_eigmin(int n, const T* Z, T* Q, T* a, T* bb, T* w, T* coef, SharedState& sh, int* steps) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // deterministic pseudo-random start vector
   double nrm2 = 0.0;
@@ -251,6 +267,7 @@ __device__ T lanczos_eigmin(int n, const T* Z, T* Q, T* a, T* bb, T* w, T* coef,
     for (int i = threadIdx.x; i < n; i += NTHREADS) Q[i] *= inv;
     __syncthreads();
   }
+  *steps = 0;
   T theta = (T)0, theta_prev = (T)INFINITY;
   T znorm = (T)0;
   int k = 0;
@@ -300,6 +317,7 @@ __device__ T lanczos_eigmin(int n, const T* Z, T* Q, T* a, T* bb, T* w, T* coef,
     for (int i = threadIdx.x; i < n; i += NTHREADS) bn += (double)w[i] * w[i];
     bn = sqrt(block_sum(bn, &sh.rb));
     k = j + 1;
+    *steps = k;
     if (threadIdx.x == 0) {
       znorm = fmax(znorm, fabs(a[j]) + (T)bn + (j > 0 ? fabs(bb[j]) : (T)0));
       if (j + 1 <= n) bb[j + 1] = (T)bn;
@@ -331,6 +349,15 @@ __device__ T lanczos_eigmin(int n, const T* Z, T* Q, T* a, T* bb, T* w, T* coef,
   return theta;
 }
 
+// (j, k) with j >= k of the idx-th entry of a packed lower triangle (row major).
+__device__ __forceinline__ void tri_index(int64_t idx, int& j, int& k) {
+  int r = (int)((sqrt(8.0 * (double)idx + 1.0) - 1.0) * 0.5);
+  while ((int64_t)(r + 1) * (r + 2) / 2 <= idx) ++r;
+  while ((int64_t)r * (r + 1) / 2 > idx) --r;
+  j = r;
+  k = (int)(idx - (int64_t)r * (r + 1) / 2);
+}
+
 // ------------------------------------------------------------------ algorithm
 template <class T>
 struct Algo {
@@ -344,6 +371,9 @@ struct Algo {
       : B(B_), prm(B_.prm), P(P_), smem(smem_), sh(sh_) {}
 
   __device__ __forceinline__ Blk<T> blk(int i) const { return make_blk<T>(B, P, i); }
+  // the whole shared-memory scratch (callers hold nothing there)
+  __device__ __forceinline__ Scratch scr() const { return Scratch{smem, MSDP_SMEM_BYTES}; }
+  __device__ __forceinline__ int blk_index(const Blk<T>& b) const { return b.index; }
   __device__ __forceinline__ int nu() const {
     int s = P.ns;
     for (int i = 0; i < P.nblocks; ++i) s += B.blk[B.prob[P.p].blk0 + i].n;
@@ -412,38 +442,66 @@ struct Algo {
   }
 
   // ---------------- _prepare! (src/primal_dual.jl:29-37)
-  __device__ bool prepare_block(const Blk<T>& b) {
-    // src/blocks.jl:126-130: Ls = chol(S) with flush, Si = S^-1
-    if (!chol_factor<T, double>(b.n, b.S, b.W(W_LS), true, smem, sh)) return false;
-    tri_inverse<T>(b.n, b.W(W_LS), b.W(W_LSI), smem);
-    // Si = Ls^-T Ls^-1 (potri)
-    cta_gemm<T>(b.n, 1, 0, 1, 1, (T)1, b.W(W_LSI), b.W(W_LSI), (T)0, b.W(W_SI));
-    cta_symmetrize<T>(b.n, b.W(W_SI));
-    return true;
-  }
-
-  // NT scaling (src/directions.jl:45-75): Lx, M = Ls' Lx, SVD of M by
-  // one-sided Jacobi (M V = U diag(D), so N = M'M = V diag(D)^2 V'),
-  // G = Lx V D^-1/2, Gi = D^1/2 V' Lx^-1, W = G G'.
+  // NT scaling (src/directions.jl:45-75).  With M = Ls' Lx and the
+  // one-sided Jacobi SVD M V = U diag(D) (so N = M'M = V diag(D)^2 V'), the
+  // rotations are also applied to Lx, which yields Lx V directly; then
+  //   G  = Lx V D^-1/2,   Gi = D^1/2 V' Lx^-1 = D^-3/2 (M V)' Ls',
+  //   W  = G G',          S^-1 = G D^-1 G'   (since G' S G = D),
+  // so no triangular inverse is needed.
   __noinline__ __device__ bool prepare_nt(const Blk<T>& b) {
     const int n = b.n;
     const int64_t nn = b.nn;
     T* M = b.W(W_T1);
-    T* V = b.W(W_T2);
+    T* GV = b.W(W_G);
     T* D = b.V(WV_D);
-    cta_gemm<T>(n, 1, 0, 1, 1, (T)1, b.W(W_LS), b.W(W_LX), (T)0, M);
+    cta_gemm<T>(n, 1, 0, 1, 1, (T)1, b.W(W_LS), b.W(W_LX), (T)0, M, scr());
     bool conv;
-    if (2 * nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) {
-      T* sM = (T*)smem;
-      T* sV = sM + nn;
-      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) sM[k] = M[k];
+    int sweeps = 0;
+    PROF_BEGIN(j);
+    if (sizeof(T) == 8 && prm.precision == MSDP_MIXED && 2 * nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) {
+      // FP64 phase of the mixed path: eigenvectors by FP32 Jacobi, then
+      // M V and Lx V in FP64 and a few FP64 polishing sweeps (quadratic
+      // convergence from the FP32 basis).
+      const Blk<float> bf = make_blk<float>(B, P, blk_index(b));
+      float* sMf = (float*)smem;
+      float* sVf = sMf + nn;
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+        sMf[k] = (float)M[k];
+        sVf[k] = ((k % n) == (k / n)) ? 1.0f : 0.0f;
+      }
       __syncthreads();
-      conv = cta_jacobi_svd<T>(n, sM, sV, D, 40, &sh.counter);
-      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) V[k] = sV[k];
+      int sw32 = 0;
+      cta_jacobi_svd<float>(n, sMf, sVf, bf.V(WV_D), 40, &sh.counter, &sw32);
+      T* V64 = b.W(W_T2);
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) V64[k] = (T)sVf[k];
+      __syncthreads();
+      T* sM = (T*)smem;
+      T* sB = sM + nn;
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, M, V64, (T)0, sM, Scratch{nullptr, 0});
+      cta_gemm<T>(n, 0, 0, 1, 0, (T)1, b.W(W_LX), V64, (T)0, sB, Scratch{nullptr, 0});
+      conv = cta_jacobi_svd<T>(n, sM, sB, D, 40, &sh.counter, &sweeps);
+      sweeps += 1000 * sw32;
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) { M[k] = sM[k]; GV[k] = sB[k]; }
+      __syncthreads();
+    } else if (2 * nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) {
+      T* sM = (T*)smem;
+      T* sB = sM + nn;
+      const T* Lx = b.W(W_LX);
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) { sM[k] = M[k]; sB[k] = Lx[k]; }
+      __syncthreads();
+      conv = cta_jacobi_svd<T>(n, sM, sB, D, 40, &sh.counter, &sweeps);
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) { M[k] = sM[k]; GV[k] = sB[k]; }
       __syncthreads();
     } else {
-      conv = cta_jacobi_svd<T>(n, M, V, D, 40, &sh.counter);
+      const T* Lx = b.W(W_LX);
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) GV[k] = Lx[k];
+      __syncthreads();
+      conv = cta_jacobi_svd<T>(n, M, GV, D, 40, &sh.counter, &sweeps);
     }
+    PROF_END(j, SC_T_JACOBI);
+    PROF_COUNT(SC_N_JACOBI_SWEEPS, sweeps);
+    PROF_COUNT(SC_N_JACOBI_CALLS, 1);
+    PROF_BEGIN(np);
     if (threadIdx.x == 0) {
       int bad = conv ? 0 : 1;
       for (int k = 0; k < n; ++k)
@@ -452,40 +510,57 @@ struct Algo {
     }
     __syncthreads();
     if (sh.flag) return false;
-    // G = Lx V, then column scaling by D^-1/2
-    cta_gemm<T>(n, 0, 0, 1, 0, (T)1, b.W(W_LX), V, (T)0, b.W(W_G));
-    // Gi = V' Lx^-1, then row scaling by D^1/2
-    cta_gemm<T>(n, 1, 0, 0, 1, (T)1, V, b.W(W_LXI), (T)0, b.W(W_GI));
-    {
-      T* G = b.W(W_G);
-      T* Gi = b.W(W_GI);
-      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
-        const int i = (int)(k % n), j = (int)(k / n);
-        G[k] = G[k] / Num<T>::sqrt_(D[j]);
-        Gi[k] = Gi[k] * Num<T>::sqrt_(D[i]);
-      }
-      __syncthreads();
+    T* G = GV;
+    T* t2 = b.W(W_T2);
+    for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+      const int j = (int)(k / n);
+      const T sq = Num<T>::sqrt_(D[j]);
+      G[k] = G[k] / sq;                 // G = Lx V D^-1/2
+      M[k] = M[k] / (D[j] * sq);        // (M V) D^-3/2
     }
-    cta_gemm<T>(n, 0, 1, 0, 0, (T)1, b.W(W_G), b.W(W_G), (T)0, b.W(W_W));
+    __syncthreads();
+    // Gi = ((M V) D^-3/2)' Ls'
+    cta_gemm<T>(n, 1, 1, 0, 1, (T)1, M, b.W(W_LS), (T)0, b.W(W_GI), scr());
+    cta_gemm<T>(n, 0, 1, 0, 0, (T)1, G, G, (T)0, b.W(W_W), scr());
     cta_symmetrize<T>(n, b.W(W_W));
+    // S^-1 = G D^-1 G'
+    for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) t2[k] = G[k] / D[k / n];
+    __syncthreads();
+    cta_gemm<T>(n, 0, 1, 0, 0, (T)1, t2, G, (T)0, b.W(W_SI), scr());
+    cta_symmetrize<T>(n, b.W(W_SI));
+    PROF_END(np, SC_T_NTPROD);
     return true;
   }
 
   __noinline__ __device__ bool prepare() {
     for (int i = 0; i < P.nblocks; ++i) {
       Blk<T> b = blk(i);
-      if (!prepare_block(b)) return false;
+      // Ls = chol(S) with flush (src/blocks.jl:94-113,126-130)
+      PROF_BEGIN(c);
+      bool ok = chol_factor<T, double>(b.n, b.S, b.W(W_LS), true, smem, sh);
+      PROF_END(c, SC_T_CHOL);
+      if (!ok) return false;
       const bool need_lx = is_nt() || prm.step == MSDP_EIGEN_STEP;
       if (need_lx) {
         // Lx = chol(X) (src/directions.jl:46 and src/step.jl:177; computed once)
-        if (!chol_factor<T, double>(b.n, b.X, b.W(W_LX), true, smem, sh)) return false;
-        tri_inverse<T>(b.n, b.W(W_LX), b.W(W_LXI), smem);
+        PROF_BEGIN(cx);
+        ok = chol_factor<T, double>(b.n, b.X, b.W(W_LX), true, smem, sh);
+        PROF_END(cx, SC_T_CHOL);
+        if (!ok) return false;
       }
       if (is_nt()) {
         if (!prepare_nt(b)) return false;
+      } else {
+        // S^-1 = Ls^-T Ls^-1 (potri, src/blocks.jl:116-123)
+        PROF_BEGIN(t);
+        tri_inverse<T>(b.n, b.W(W_LS), b.W(W_LSI), smem);
+        cta_gemm<T>(b.n, 1, 0, 1, 1, (T)1, b.W(W_LSI), b.W(W_LSI), (T)0, b.W(W_SI), scr());
+        cta_symmetrize<T>(b.n, b.W(W_SI));
+        if (prm.step == MSDP_EIGEN_STEP) tri_inverse<T>(b.n, b.W(W_LX), b.W(W_LXI), smem);
+        PROF_END(t, SC_T_TRTRI);
+        // the compute-type view of X used by HKM's E(.) and Schur scaling
+        (void)as_T<T>(b.nn, b.X, b.W(W_XT));
       }
-      // the compute-type view of X used by HKM's E(.) and Schur scaling
-      if (!is_nt()) (void)as_T<T>(b.nn, b.X, b.W(W_XT));
     }
     for (int k = threadIdx.x; k < P.ns; k += NTHREADS) P.zinv[k] = 1.0 / P.z[k];
     __syncthreads();
@@ -512,10 +587,29 @@ struct Algo {
       L = sL;
       R = sR;
     }
-    const int64_t mm = (int64_t)m * m;
-    for (int64_t idx = threadIdx.x; idx < mm; idx += NTHREADS) {
-      const int j = (int)(idx % m), k = (int)(idx / m);
-      if (j < k) continue;
+    const int64_t npairs = (int64_t)m * (m + 1) / 2;
+    if (b.structure == STRUCT_HANKEL) {
+      // A_j = sum_{a+b=j} E_ab (0/1): H_jk = sum_a sum_c L[a,c] R[k-c, j-a]
+      for (int64_t idx = threadIdx.x; idx < npairs; idx += NTHREADS) {
+        int j, k;
+        tri_index(idx, j, k);
+        const int a0 = max(0, j - n + 1), a1 = min(j, n - 1);
+        const int c0 = max(0, k - n + 1), c1 = min(k, n - 1);
+        T acc = (T)0;
+        for (int a = a0; a <= a1; ++a) {
+          const T* Ra = R + (int64_t)(j - a) * n + k;   // R[k-c, j-a] = Ra[-c]
+          const T* La = L + a;                          // L[a, c] = La[c*n]
+          for (int c = c0; c <= c1; ++c) acc = fma(La[(int64_t)c * n], Ra[-c], acc);
+        }
+        H[j + (int64_t)k * m] += acc;
+        if (j != k) H[k + (int64_t)j * m] += acc;
+      }
+      __syncthreads();
+      return;
+    }
+    for (int64_t idx = threadIdx.x; idx < npairs; idx += NTHREADS) {
+      int j, k;
+      tri_index(idx, j, k);
       const int64_t e0 = b.cptr[j], e1 = b.cptr[j + 1];
       const int64_t f0 = b.cptr[k], f1 = b.cptr[k + 1];
       T acc = (T)0;
@@ -575,7 +669,11 @@ struct Algo {
     T* L = schur_L();
     double reg = prm.regularize_schur;
     for (int attempt = 0; attempt < prm.max_schur_reg; ++attempt) {
+      PROF_BEGIN(a);
       schur_complement(H);
+      PROF_END(a, SC_T_ASSEMBLY);
+      PROF_COUNT(SC_N_FACTOR, 1);
+      PROF_BEGIN(f);
       if (reg > 0.0) {
         for (int i = threadIdx.x; i < m; i += NTHREADS) H[i + (int64_t)i * m] += (T)reg;
         __syncthreads();
@@ -591,8 +689,10 @@ struct Algo {
           for (int64_t k = threadIdx.x; k < mm; k += NTHREADS) L[k] = A[k];
           __syncthreads();
         }
+        PROF_END(f, SC_T_FACTOR);
         return true;
       }
+      PROF_END(f, SC_T_FACTOR);
       reg = (reg == 0.0) ? 1e-12 : 10.0 * reg;
     }
     return false;
@@ -607,11 +707,11 @@ struct Algo {
     const int n = b.n;
     T* tmp = b.W(W_T3);
     if (is_nt()) {
-      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_W), Min, (T)0, tmp);
-      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, tmp, b.W(W_W), (T)0, out);
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_W), Min, (T)0, tmp, scr());
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, tmp, b.W(W_W), (T)0, out, scr());
     } else {
-      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, xt(b), Min, (T)0, tmp);
-      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, tmp, b.W(W_SI), (T)0, out);
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, xt(b), Min, (T)0, tmp, scr());
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, tmp, b.W(W_SI), (T)0, out, scr());
     }
     cta_symmetrize<T>(n, out);
   }
@@ -702,19 +802,19 @@ struct Algo {
       if (is_nt()) {
         T* RNT = b.W(W_RNT);
         const T* D = b.V(WV_D);
-        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_GI), dxt, (T)0, t1);
-        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, t1, dst, (T)0, t2);
-        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, t2, b.W(W_G), (T)0, t3);
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_GI), dxt, (T)0, t1, scr());
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, t1, dst, (T)0, t2, scr());
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, t2, b.W(W_G), (T)0, t3, scr());
         for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) {
           const int p = (int)(k % n), q = (int)(k / n);
           RNT[k] = -(t3[k] + t3[q + (int64_t)p * n]) / (D[p] + D[q]);
         }
         __syncthreads();
-        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_G), RNT, (T)0, t1);
-        cta_gemm<T>(n, 0, 1, 0, 0, (T)1, t1, b.W(W_G), (T)0, corr);
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_G), RNT, (T)0, t1, scr());
+        cta_gemm<T>(n, 0, 1, 0, 0, (T)1, t1, b.W(W_G), (T)0, corr, scr());
       } else {
-        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, dxt, dst, (T)0, t1);
-        cta_gemm<T>(n, 0, 0, 0, 0, (T)-1, t1, b.W(W_SI), (T)0, corr);
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, dxt, dst, (T)0, t1, scr());
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)-1, t1, b.W(W_SI), (T)0, corr, scr());
       }
       cta_symmetrize<T>(n, corr);
     }
@@ -731,26 +831,103 @@ struct Algo {
     return -block_max(-a, &sh.rb);
   }
 
-  // Fraction tau of the largest step keeping L L' + a D positive definite,
-  // from the smallest eigenvalue of L^-1 D L^-T (src/step.jl:178-183).
-  __noinline__ __device__ double eigen_step(const Blk<T>& b, const T* Li, const double* Dm, double tau) {
+  // Fraction tau of the largest step keeping X + a dX and S + b dS positive
+  // definite, from the smallest eigenvalues of L^-1 D L^-T (src/step.jl:178-183).
+  // NT forms them in the scaled space (X = G D G', S = Gi' D Gi):
+  //   Z_X = D^-1/2 Gi dX Gi' D^-1/2,  Z_S = D^-1/2 G' dS G D^-1/2,
+  // which are congruent to Lx^-1 dX Lx^-T and Ls^-1 dS Ls^-T; HKM uses the
+  // triangular inverses.  Warp 0 and warp 1 run the two Lanczos iterations
+  // concurrently.
+  __noinline__ __device__ void eigen_steps(const Blk<T>& b, double tau, double& ax, double& as) {
     const int n = b.n;
-    T* dt = as_T<T>(b.nn, Dm, b.W(W_DXT));
-    T* t1 = b.W(W_T1);
-    T* Z = b.W(W_T2);
-    cta_gemm<T>(n, 0, 0, 1, 0, (T)1, Li, dt, (T)0, t1);
-    cta_gemm<T>(n, 0, 1, 0, 1, (T)1, t1, Li, (T)0, Z);
-    const T* Zs = Z;
     const int64_t nn = b.nn;
-    if (nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) {
-      T* sZ = (T*)smem;
-      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) sZ[k] = Z[k];
+    T* dxt = as_T<T>(nn, b.dX, b.W(W_DXT));
+    T* dst = as_T<T>(nn, b.dS, b.W(W_DST));
+    T* t1 = b.W(W_T1);
+    T* ZX = b.W(W_T2);
+    T* ZS = b.W(W_T3);
+    if (is_nt()) {
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_GI), dxt, (T)0, t1, scr());
+      cta_gemm<T>(n, 0, 1, 0, 0, (T)1, t1, b.W(W_GI), (T)0, ZX, scr());
+      cta_gemm<T>(n, 1, 0, 0, 0, (T)1, b.W(W_G), dst, (T)0, t1, scr());
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, t1, b.W(W_G), (T)0, ZS, scr());
+      const T* D = b.V(WV_D);
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+        const T sc = Num<T>::rsqrt_(D[k % n]) * Num<T>::rsqrt_(D[k / n]);
+        ZX[k] *= sc;
+        ZS[k] *= sc;
+      }
       __syncthreads();
-      Zs = sZ;
+    } else {
+      cta_gemm<T>(n, 0, 0, 1, 0, (T)1, b.W(W_LXI), dxt, (T)0, t1, scr());
+      cta_gemm<T>(n, 0, 1, 0, 1, (T)1, t1, b.W(W_LXI), (T)0, ZX, scr());
+      cta_gemm<T>(n, 0, 0, 1, 0, (T)1, b.W(W_LSI), dst, (T)0, t1, scr());
+      cta_gemm<T>(n, 0, 1, 0, 1, (T)1, t1, b.W(W_LSI), (T)0, ZS, scr());
     }
-    const T lam = lanczos_eigmin<T>(n, Zs, b.W(W_Q), b.V(WV_LA), b.V(WV_LB), b.V(WV_LW), b.V(WV_LC), sh);
-    const double l = (double)lam;
-    return l > -sqrt(2.220446049250313e-16) ? 1.0 : fmin(1.0, -tau / l);
+    PROF_BEGIN(l);
+    int steps = 0;
+    if (n <= 256) {
+      // per Lanczos: Z (n^2), kq basis columns and 4 vectors in shared memory
+      const int64_t vec = 4 * (int64_t)(n + 1);
+      const int64_t cap = MSDP_SMEM_BYTES / (int64_t)sizeof(T);
+      int kq2 = (int)min((int64_t)n, max((int64_t)0, (cap / 2 - nn - vec) / n));   // two concurrent
+      int kq1 = (int)min((int64_t)n, max((int64_t)0, (cap - nn - vec) / n));       // one at a time
+      const bool concurrent = kq2 >= min(n, 16);
+      const int kq = concurrent ? kq2 : kq1;
+      const bool staged = (kq >= 1);
+      const int64_t per = nn + (int64_t)kq * n + vec;
+      T* base0 = (T*)smem;
+      T* base1 = concurrent ? base0 + per : base0;
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int pass = 0; pass < (concurrent || !staged ? 1 : 2); ++pass) {
+        // stage the Z matrices this pass needs
+        if (staged) {
+          if (concurrent || pass == 0)
+            for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) base0[k] = ZX[k];
+          if (concurrent || pass == 1)
+            for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) base1[k] = ZS[k];
+          __syncthreads();
+        }
+        const bool runx = (concurrent || !staged) ? (warp == 0) : (pass == 0 && warp == 0);
+        const bool runs = (concurrent || !staged) ? (warp == 1) : (pass == 1 && warp == 0);
+        if (runx) {
+          T* bs = base0;
+          const T* z = staged ? bs : ZX;
+          T* v = staged ? bs + nn + (int64_t)kq * n : b.V(WV_LA);
+          const T lam = staged
+              ? warp_lanczos_eigmin<T>(n, z, bs + nn, kq, b.W(W_Q), v, v + (n + 1), v + 2 * (n + 1), v + 3 * (n + 1), &steps)
+              : warp_lanczos_eigmin<T>(n, z, b.W(W_Q), n, b.W(W_Q), b.V(WV_LA), b.V(WV_LB), b.V(WV_LW), b.V(WV_LC), &steps);
+          if (lane == 0) { sh.bc[2] = (double)lam; sh.bc[4] = (double)steps; }
+        } else if (runs) {
+          T* bs = base1;
+          const T* z = staged ? bs : ZS;
+          T* v = staged ? bs + nn + (int64_t)kq * n : b.V(WV_LA2);
+          const T lam = staged
+              ? warp_lanczos_eigmin<T>(n, z, bs + nn, kq, b.W(W_RNT), v, v + (n + 1), v + 2 * (n + 1), v + 3 * (n + 1), &steps)
+              : warp_lanczos_eigmin<T>(n, z, b.W(W_RNT), n, b.W(W_RNT), b.V(WV_LA2), b.V(WV_LB2), b.V(WV_LW2), b.V(WV_LC2), &steps);
+          if (lane == 0) { sh.bc[3] = (double)lam; sh.bc[5] = (double)steps; }
+        }
+        __syncthreads();
+      }
+      steps = (int)(sh.bc[4] + sh.bc[5]);
+    } else {
+      const T* zx = ZX;
+      const T* zs = ZS;
+      int s1 = 0, s2 = 0;
+      const T lx = lanczos_eigmin<T>(n, zx, b.W(W_Q), b.V(WV_LA), b.V(WV_LB), b.V(WV_LW), b.V(WV_LC), sh, &s1);
+      const T ls = lanczos_eigmin<T>(n, zs, b.W(W_RNT), b.V(WV_LA2), b.V(WV_LB2), b.V(WV_LW2), b.V(WV_LC2), sh, &s2);
+      if (threadIdx.x == 0) { sh.bc[2] = (double)lx; sh.bc[3] = (double)ls; }
+      __syncthreads();
+      steps = s1 + s2;
+    }
+    PROF_END(l, SC_T_LANCZOS);
+    PROF_COUNT(SC_N_LANCZOS_STEPS, steps);
+    PROF_COUNT(SC_N_LANCZOS_CALLS, 2);
+    const double lx = sh.bc[2], ls = sh.bc[3];
+    __syncthreads();
+    const double thr = -sqrt(2.220446049250313e-16);
+    ax = lx > thr ? 1.0 : fmin(1.0, -tau / lx);
+    as = ls > thr ? 1.0 : fmin(1.0, -tau / ls);
   }
 
   __noinline__ __device__ double backtrack(bool primal) {
@@ -775,8 +952,10 @@ struct Algo {
       a = 1.0; bt = 1.0;
       for (int i = 0; i < P.nblocks; ++i) {
         Blk<T> b = blk(i);
-        a = fmin(a, eigen_step(b, b.W(W_LXI), b.dX, prm.tau));
-        bt = fmin(bt, eigen_step(b, b.W(W_LSI), b.dS, prm.tau));
+        double ax, as;
+        eigen_steps(b, prm.tau, ax, as);
+        a = fmin(a, ax);
+        bt = fmin(bt, as);
       }
       if (P.ns > 0) {
         a = fmin(a, prm.tau * max_scalar_step(P.x, P.delx));
@@ -841,12 +1020,18 @@ struct Algo {
     update_residuals();
   }
 
-  __device__ void solve_directions(double mu, bool corrected) {
+  __noinline__ __device__ void solve_directions(double mu, bool corrected) {
+    PROF_BEGIN(r);
     rhs(mu, corrected);
     for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.dely[j] = P.h[j];
     __syncthreads();
+    PROF_END(r, SC_T_RHS);
+    PROF_BEGIN(s);
     schur_solve(P.dely);
+    PROF_END(s, SC_T_SOLVE);
+    PROF_BEGIN(d);
     directions(mu, corrected);
+    PROF_END(d, SC_T_DIRECTIONS);
   }
 
   // One Mehrotra predictor-corrector iteration (src/primal_dual.jl:85-101).
@@ -858,17 +1043,31 @@ struct Algo {
     __syncthreads();
     solve_directions(0.0, false);
     double a_aff, b_aff;
-    step_lengths(a_aff, b_aff);
+    {
+      PROF_BEGIN(st);
+      step_lengths(a_aff, b_aff);
+      PROF_END(st, SC_T_STEP);
+    }
     const double mu_aff = affine_complementarity(a_aff, b_aff);
     const double sigma = fmin(fmax(pow(mu_aff / fmax(mu, 2.220446049250313e-16), prm.sigma_exponent), 1e-8), 1.0);
     if (threadIdx.x == 0) P.sc[SC_SIGMA] = sigma;
     __syncthreads();
-    correction();
+    {
+      PROF_BEGIN(c);
+      correction();
+      PROF_END(c, SC_T_CORRECTION);
+    }
     solve_directions(sigma * mu, true);
     double a, bt;
-    step_lengths(a, bt);
+    {
+      PROF_BEGIN(st);
+      step_lengths(a, bt);
+      PROF_END(st, SC_T_STEP);
+    }
     if (!strict && !(fmin(a, bt) >= 0.2)) return false;
+    PROF_BEGIN(tk);
     take_step(a, bt);
+    PROF_END(tk, SC_T_TAKE);
     return true;
   }
 
@@ -902,8 +1101,26 @@ template <> __device__ __forceinline__ double* Algo<double>::schur_L() { return 
 template <> __device__ __forceinline__ float* Algo<float>::schur_H() { return P.Hf; }
 template <> __device__ __forceinline__ float* Algo<float>::schur_L() { return P.Lf; }
 
+// Stage the right-hand side (and the factor when it fits) in shared memory
+// and solve with one warp.
+template <class T>
+__device__ void staged_potrs(int m, const T* L, double* x, unsigned char* smem) {
+  const int64_t mm = (int64_t)m * m;
+  double* sx = (double*)smem;
+  T* sL = (T*)(smem + (((int64_t)m * sizeof(double) + 15) & ~(int64_t)15));
+  const bool stageL = ((int64_t)m * sizeof(double) + 16 + mm * (int64_t)sizeof(T)) <= MSDP_SMEM_BYTES;
+  for (int j = threadIdx.x; j < m; j += NTHREADS) sx[j] = x[j];
+  if (stageL)
+    for (int64_t k = threadIdx.x; k < mm; k += NTHREADS) sL[k] = L[k];
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0) warp_potrs<T, double>(m, stageL ? sL : L, sx);
+  __syncthreads();
+  for (int j = threadIdx.x; j < m; j += NTHREADS) x[j] = sx[j];
+  __syncthreads();
+}
+
 template <> __device__ void Algo<double>::schur_solve(double* x) {
-  cta_potrs<double, double>(P.m, P.H64, x);
+  staged_potrs<double>(P.m, P.H64, x, smem);
 }
 
 template <> __device__ void Algo<float>::schur_solve(double* x) {
@@ -914,7 +1131,7 @@ template <> __device__ void Algo<float>::schur_solve(double* x) {
   double* r = P.wm2;  // residual / correction
   for (int j = threadIdx.x; j < m; j += NTHREADS) { h[j] = x[j]; r[j] = x[j]; }
   __syncthreads();
-  cta_potrs<float, double>(m, P.Lf, r);
+  staged_potrs<float>(m, P.Lf, r, smem);
   for (int j = threadIdx.x; j < m; j += NTHREADS) x[j] = r[j];
   __syncthreads();
   for (int it = 0; it < 2; ++it) {
@@ -924,7 +1141,7 @@ template <> __device__ void Algo<float>::schur_solve(double* x) {
       r[j] = s;
     }
     __syncthreads();
-    cta_potrs<float, double>(m, P.Lf, r);
+    staged_potrs<float>(m, P.Lf, r, smem);
     for (int j = threadIdx.x; j < m; j += NTHREADS) x[j] += r[j];
     __syncthreads();
   }

@@ -150,6 +150,7 @@ __device__ bool initialize(const BatchDev& B, Prob& P, unsigned char* smem, Shar
     P.sc[SC_N32] = 0.0; P.sc[SC_N64] = 0.0;
     P.sc[SC_ALPHA] = 0.0; P.sc[SC_BETA] = 0.0; P.sc[SC_SIGMA] = 0.0;
     P.sc[SC_INFPR] = INFINITY; P.sc[SC_INFDU] = INFINITY; P.sc[SC_GAP] = INFINITY;
+    for (int k = SC_T_CHOL; k < SC_PROFILE_END; ++k) { P.sc[k] = 0.0; P.sc[k + SC_PROFILE_F64] = 0.0; }
   }
   __syncthreads();
   // initialize_algorithm!(solver, ::PrimalDual)
@@ -169,10 +170,23 @@ __device__ void iterate_one(const BatchDev& B, Prob& P, unsigned char* smem, Sha
     int phase = (int)P.sc[SC_PHASE];
     if (phase == 0 && fmax(fmax(P.sc[SC_INFPR], P.sc[SC_INFDU]), P.sc[SC_GAP]) < prm.switch_tol) phase = 1;
     if (phase == 0) {
+      const double pr_old = P.sc[SC_INFPR];
       Algo<float> A(B, P, smem, sh);
       const bool ok = A.iterate_pd(false);
       if (ok) {
-        if (threadIdx.x == 0) P.sc[SC_N32] += 1.0;
+        // The dual residual update is exact in float64 (dS = Rd - A*(dy));
+        // the primal one is not: Rp_new = (1 - a) Rp - a (A(dX) - Rp).  If
+        // the estimated error of the FP32 direction exceeds 10% of the
+        // residual it had to remove, later iterations run in FP64.
+        double rp = 0.0;
+        for (int j = threadIdx.x; j < P.m; j += NTHREADS) rp = fmax(rp, fabs(P.Rp[j]));
+        rp = block_max(rp, &sh.rb) / fmax(1.0, P.sc[SC_BNORM]);
+        const double a = P.sc[SC_ALPHA];
+        const double err = fmax(0.0, rp - (1.0 - a) * pr_old) / fmax(a, 1e-300);
+        if (threadIdx.x == 0) {
+          P.sc[SC_N32] += 1.0;
+          if (err > 0.1 * pr_old) P.sc[SC_PHASE] = 1.0;
+        }
         __syncthreads();
         return;
       }
@@ -207,9 +221,13 @@ __device__ void run_op(const BatchDev& B, Prob& P, unsigned char* smem, SharedSt
     case OP_ITERATE: {
       for (int k = 0; (prm.max_iterations <= 0 || k < prm.max_iterations) && k < 1000000; ++k) {
         if ((int)P.sc[SC_STATUS] != MSDP_REGULAR) break;
+        const long long t_it = clock64();
         iterate_one<MIXED>(B, P, smem, sh);
+        if (threadIdx.x == 0) P.sc[SC_T_ITER] += (double)(clock64() - t_it);
         if ((int)P.sc[SC_STATUS] != MSDP_REGULAR) break;
+        const long long t_tm = clock64();
         update_termination(B, P, smem, sh);
+        if (threadIdx.x == 0) P.sc[SC_T_TERM] += (double)(clock64() - t_tm);
       }
       break;
     }
@@ -241,7 +259,7 @@ __device__ void run_op(const BatchDev& B, Prob& P, unsigned char* smem, SharedSt
 }
 
 template <int MIXED>
-__global__ void __launch_bounds__(NTHREADS, 1) msdp_ipm_kernel(const __grid_constant__ BatchDev B) {
+__global__ void __launch_bounds__(NTHREADS, 3) msdp_ipm_kernel(const __grid_constant__ BatchDev B) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ SharedState sh;
   for (;;) {

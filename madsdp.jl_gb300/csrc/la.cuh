@@ -10,7 +10,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#define NTHREADS 256
+#ifndef NTHREADS
+#define NTHREADS 128
+#endif
 #define NWARPS (NTHREADS / 32)
 
 template <class T> struct Num;
@@ -171,10 +173,38 @@ __device__ void cta_gemm_r(int n, int ta, int tb, int loA, int loB, T alpha, con
 }
 
 template <class T>
-__device__ __forceinline__ void cta_gemm(int n, int ta, int tb, int loA, int loB, T alpha, const T* A,
-                                         const T* B, T beta, T* C) {
+__device__ __forceinline__ void cta_gemm_plain(int n, int ta, int tb, int loA, int loB, T alpha, const T* A,
+                                               const T* B, T beta, T* C) {
   if (n <= 24) cta_gemm_r<T, 2>(n, ta, tb, loA, loB, alpha, A, B, beta, C);
   else cta_gemm_r<T, 4>(n, ta, tb, loA, loB, alpha, A, B, beta, C);
+}
+
+// Shared-memory scratch handed to the routines that stage operands
+// (nullptr / 0 bytes: operate in global memory).
+struct Scratch {
+  unsigned char* p;
+  int64_t bytes;
+};
+
+// GEMM whose operands are first copied into shared memory when they fit
+// (operands written earlier by this CTA would otherwise be re-read from L2).
+template <class T>
+__device__ void cta_gemm(int n, int ta, int tb, int loA, int loB, T alpha, const T* A, const T* B, T beta, T* C,
+                         Scratch sc) {
+  const int64_t nn = (int64_t)n * n;
+  const int64_t need = (A == B ? 1 : 2) * nn * (int64_t)sizeof(T);
+  if (sc.p != nullptr && need <= sc.bytes) {
+    T* sA = (T*)sc.p;
+    T* sB = (A == B) ? sA : sA + nn;
+    for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+      sA[k] = A[k];
+      if (A != B) sB[k] = B[k];
+    }
+    __syncthreads();
+    cta_gemm_plain<T>(n, ta, tb, loA, loB, alpha, sA, sB, beta, C);
+  } else {
+    cta_gemm_plain<T>(n, ta, tb, loA, loB, alpha, A, B, beta, C);
+  }
 }
 
 // ---------------------------------------------------------------- Cholesky
@@ -278,68 +308,106 @@ __device__ void cta_potrs(int n, const T* __restrict__ L, V* x) {
 
 // ---------------------------------------------------------------- Jacobi SVD
 // One-sided (Hestenes) Jacobi on the columns of M (n x n, ld n): on return
-// M V has mutually orthogonal columns, V is orthogonal and sigma[k] is the
-// norm of column k of M V.  The eigenvalues of M'M are sigma^2 with
-// eigenvectors V, which is what LowRankOpt.eigen! returns for the NT
-// scaling (src/directions.jl:52-58).  Parallel round-robin ordering, one
-// warp per column pair.  Returns false if it did not converge in max_sweeps.
-template <class T>
-__device__ bool cta_jacobi_svd(int n, T* M, T* V, T* sigma, int max_sweeps, int* counter) {
-  cta_set_identity<T>(n, V, (T)1);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// M V has mutually orthogonal columns and sigma[k] is the norm of column k.
+// The eigenvalues of M'M are sigma^2 with eigenvectors V, which is what
+// LowRankOpt.eigen! returns for the NT scaling (src/directions.jl:52-58).
+// Every rotation is also applied to the columns of B (n x n): B = I gives
+// V itself, B = Lx gives Lx V directly.  Parallel round-robin ordering; each
+// column pair is handled by a group of G lanes (G = 8, 16 or 32 by n).
+// Returns false if it did not converge in max_sweeps.
+template <class T, int G>
+__device__ bool cta_jacobi_svd_g(int n, T* M, T* B, T* sigma, int max_sweeps, int* counter, int* sweeps_out) {
+  const int lane = threadIdx.x & 31;
+  const int gl = lane & (G - 1);                      // lane within its group
+  const int group = threadIdx.x / G;                  // global group index
+  constexpr int NG = NTHREADS / G;
   const int N = (n % 2 == 0) ? n : n + 1;
   const T tol = (T)sqrt((double)n) * Num<T>::eps();
   bool converged = (n <= 1);
-  for (int sweep = 0; sweep < max_sweeps && !converged; ++sweep) {
+  int sweep = 0;
+  for (; sweep < max_sweeps && !converged; ++sweep) {
     if (threadIdx.x == 0) *counter = 0;
     __syncthreads();
+    int rotated = 0, big = 0;
+    const T big_tol = Num<T>::sqrt_(tol);
     for (int r = 0; r < N - 1; ++r) {
-      for (int k = warp; k < N / 2; k += NWARPS) {
-        int p, q;
-        if (k == 0) { p = N - 1; q = r; }
-        else { p = (r + k) % (N - 1); q = (r - k + (N - 1)) % (N - 1); }
-        if (p >= n || q >= n) continue;
-        T* mp = M + (int64_t)p * n;
-        T* mq = M + (int64_t)q * n;
+      // every group runs the same number of pair slots so shuffles stay uniform
+      const int slots = (N / 2 + NG - 1) / NG;
+      for (int sidx = 0; sidx < slots; ++sidx) {
+        const int k = group + sidx * NG;
+        int p = -1, q = -1;
+        if (k < N / 2) {
+          if (k == 0) { p = N - 1; q = r; }
+          else { p = (r + k) % (N - 1); q = (r - k + (N - 1)) % (N - 1); }
+          if (p >= n || q >= n) { p = -1; q = -1; }
+        }
         T app = 0, aqq = 0, apq = 0;
-        for (int i = lane; i < n; i += 32) {
-          const T a = mp[i], b = mq[i];
-          app = fma(a, a, app); aqq = fma(b, b, aqq); apq = fma(a, b, apq);
+        if (p >= 0) {
+          const T* mp = M + (int64_t)p * n;
+          const T* mq = M + (int64_t)q * n;
+          for (int i = gl; i < n; i += G) {
+            const T a = mp[i], b = mq[i];
+            app = fma(a, a, app); aqq = fma(b, b, aqq); apq = fma(a, b, apq);
+          }
         }
-        app = warp_sum(app); aqq = warp_sum(aqq); apq = warp_sum(apq);
-        if (!(fabs(apq) > tol * Num<T>::sqrt_(app) * Num<T>::sqrt_(aqq))) continue;
-        const T zeta = (aqq - app) / ((T)2 * apq);
-        const T t = (zeta >= (T)0 ? (T)1 : (T)-1) / (fabs(zeta) + Num<T>::sqrt_((T)1 + zeta * zeta));
-        const T c = Num<T>::rsqrt_((T)1 + t * t), s = c * t;
-        for (int i = lane; i < n; i += 32) {
-          const T a = mp[i], b = mq[i];
-          mp[i] = c * a - s * b;
-          mq[i] = s * a + c * b;
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
+          app += __shfl_xor_sync(0xffffffffu, app, o);
+          aqq += __shfl_xor_sync(0xffffffffu, aqq, o);
+          apq += __shfl_xor_sync(0xffffffffu, apq, o);
         }
-        T* vp = V + (int64_t)p * n;
-        T* vq = V + (int64_t)q * n;
-        for (int i = lane; i < n; i += 32) {
-          const T a = vp[i], b = vq[i];
-          vp[i] = c * a - s * b;
-          vq[i] = s * a + c * b;
+        const T scale_pq = Num<T>::sqrt_(app) * Num<T>::sqrt_(aqq);
+        if (p >= 0 && fabs(apq) > tol * scale_pq) {
+          if (fabs(apq) > big_tol * scale_pq) big = 1;
+          const T zeta = (aqq - app) / ((T)2 * apq);
+          const T t = (zeta >= (T)0 ? (T)1 : (T)-1) / (fabs(zeta) + Num<T>::sqrt_((T)1 + zeta * zeta));
+          const T c = Num<T>::rsqrt_((T)1 + t * t), sn = c * t;
+          T* mp = M + (int64_t)p * n;
+          T* mq = M + (int64_t)q * n;
+          T* bp = B + (int64_t)p * n;
+          T* bq = B + (int64_t)q * n;
+          for (int i = gl; i < n; i += G) {
+            const T a = mp[i], b = mq[i];
+            mp[i] = c * a - sn * b;
+            mq[i] = sn * a + c * b;
+            const T u = bp[i], v = bq[i];
+            bp[i] = c * u - sn * v;
+            bq[i] = sn * u + c * v;
+          }
+          rotated = 1;
         }
-        if (lane == 0) atomicAdd(counter, 1);
       }
       __syncthreads();
     }
-    converged = (*counter == 0);
-    __syncthreads();
+    rotated = __syncthreads_or(rotated);
+    big = __syncthreads_or(big);
+    // quadratic convergence: after a sweep whose rotations all had
+    // |a_pq| <= sqrt(tol) sqrt(a_pp a_qq), the off-diagonals are O(tol)
+    converged = !rotated || !big;
   }
-  // column norms
-  for (int k = warp; k < n; k += NWARPS) {
-    const T* mk = M + (int64_t)k * n;
+  *sweeps_out = sweep;
+  // column norms (uniform slot count so every lane reaches every shuffle)
+  const int nslots = (n + NG - 1) / NG;
+  for (int sidx = 0; sidx < nslots; ++sidx) {
+    const int k = group + sidx * NG;
     T s = 0;
-    for (int i = lane; i < n; i += 32) s = fma(mk[i], mk[i], s);
-    s = warp_sum(s);
-    if (lane == 0) sigma[k] = Num<T>::sqrt_(s);
+    if (k < n) {
+      const T* mk = M + (int64_t)k * n;
+      for (int i = gl; i < n; i += G) s = fma(mk[i], mk[i], s);
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (k < n && gl == 0) sigma[k] = Num<T>::sqrt_(s);
   }
   __syncthreads();
   return converged;
+}
+
+template <class T>
+__device__ bool cta_jacobi_svd(int n, T* M, T* B, T* sigma, int max_sweeps, int* counter, int* sweeps_out) {
+  if (n <= 16) return cta_jacobi_svd_g<T, 8>(n, M, B, sigma, max_sweeps, counter, sweeps_out);
+  if (n <= 48) return cta_jacobi_svd_g<T, 16>(n, M, B, sigma, max_sweeps, counter, sweeps_out);
+  return cta_jacobi_svd_g<T, 32>(n, M, B, sigma, max_sweeps, counter, sweeps_out);
 }
 
 // ---------------------------------------------------------------- tridiagonal
@@ -408,4 +476,149 @@ __device__ T thread_tridiag_eig(int k, const T* a, const T* b, int j) {
     else lo = x;
   }
   return (lo + hi) / (T)2;
+}
+
+// ---------------------------------------------------------------- warp routines
+// Smallest eigenvalue of the symmetric Z (n x n) by Lanczos with full
+// reorthogonalization, run by ONE warp (the role of
+// LowRankOpt.lanczos_eigmin!, src/step.jl:151-183).  Q (n x n) holds the
+// basis; a, bb, coef are vectors of length n+1, w of length n.  Stops when
+// the smallest Ritz value is stable to 64 eps or the Krylov space is
+// exhausted (k = n or b_k ~ 0).
+template <class T>
+__device__ T warp_lanczos_eigmin(int n, const T* Z, T* Qs, int kq, T* Qg, T* a, T* bb, T* w, T* coef, int* steps) {
+  const int lane = threadIdx.x & 31;
+  // column l of the basis: shared memory for l < kq, global memory after
+  auto Qc = [&](int l) -> T* { return l < kq ? Qs + (int64_t)l * n : Qg + (int64_t)l * n; };
+  T* Q = Qc(0);
+  T nrm2 = 0;
+  for (int i = lane; i < n; i += 32) {
+    uint32_t h = (uint32_t)(i + 1) * 2654435761u;
+    h ^= h >> 15; h *= 2246822519u; h ^= h >> 13;
+    const T v = (T)((double)(h & 0xffffff) / 16777216.0 - 0.5) + (T)0.01;
+    Q[i] = v;
+    nrm2 = fma(v, v, nrm2);
+  }
+  nrm2 = warp_sum(nrm2);
+  {
+    const T inv = (T)1 / Num<T>::sqrt_(nrm2);
+    for (int i = lane; i < n; i += 32) Q[i] *= inv;
+  }
+  __syncwarp();
+  T theta = 0, theta_prev = (T)INFINITY, znorm = 0;
+  int k = 0;
+  for (int j = 0; j < n; ++j) {
+    const T* qj = Qc(j);
+    // w = Z q_j (Z symmetric; lanes read consecutive rows of each column)
+    T wl[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) wl[t] = 0;
+    for (int r = 0; r < n; ++r) {
+      const T qr = qj[r];
+      const T* zr = Z + (int64_t)r * n;
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int i = lane + 32 * t;
+        if (i < n) wl[t] = fma(zr[i], qr, wl[t]);
+      }
+    }
+    T aj = 0;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int i = lane + 32 * t;
+      if (i < n) aj = fma(qj[i], wl[t], aj);
+    }
+    aj = warp_sum(aj);
+    const T bj = j > 0 ? bb[j] : (T)0;
+    const T* qp = j > 0 ? Qc(j - 1) : qj;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int i = lane + 32 * t;
+      if (i < n) {
+        T v = wl[t] - aj * qj[i];
+        if (j > 0) v -= bj * qp[i];
+        wl[t] = v;
+        w[i] = v;
+      }
+    }
+    if (lane == 0) a[j] = aj;
+    __syncwarp();
+    // full reorthogonalization, twice: coef_l = Q_l . w (one lane per l)
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int l = lane; l <= j; l += 32) {
+        const T* ql = Qc(l);
+        T s = 0;
+        for (int i = 0; i < n; ++i) s = fma(ql[i], w[i], s);
+        coef[l] = s;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int i = lane + 32 * t;
+        if (i < n) {
+          T v = wl[t];
+          for (int l = 0; l <= j; ++l) v = fma(-coef[l], Qc(l)[i], v);
+          wl[t] = v;
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int i = lane + 32 * t;
+        if (i < n) w[i] = wl[t];
+      }
+      __syncwarp();
+    }
+    T bn = 0;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int i = lane + 32 * t;
+      if (i < n) bn = fma(wl[t], wl[t], bn);
+    }
+    bn = Num<T>::sqrt_(warp_sum(bn));
+    k = j + 1;
+    znorm = fmax(znorm, fabs(aj) + bn + fabs(bj));
+    if (lane == 0) bb[j + 1] = bn;
+    __syncwarp();
+    const bool exhausted = (k == n) || !(bn > Num<T>::eps() * znorm * (T)4);
+    if (exhausted || (k >= 4 && (k % 4) == 0)) {
+      theta = warp_tridiag_eigmin<T>(k, a, bb);
+      const T tolr = Num<T>::eps() * (T)64 * fmax((T)1, fabs(theta));
+      if (exhausted || fabs(theta - theta_prev) <= tolr) break;
+      theta_prev = theta;
+    }
+    T* qn = Qc(j + 1);
+    const T inv = (T)1 / bn;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int i = lane + 32 * t;
+      if (i < n) qn[i] = wl[t] * inv;
+    }
+    __syncwarp();
+  }
+  *steps = k;
+  return theta;
+}
+
+// Solve L L' x = b in place (L lower, ld m) by ONE warp; x (and L, when
+// the caller staged it) in shared memory.
+template <class T, class V>
+__device__ void warp_potrs(int m, const T* __restrict__ L, V* x) {
+  const int lane = threadIdx.x & 31;
+  for (int k = 0; k < m; ++k) {
+    const V xk = x[k] / (V)L[k + (int64_t)k * m];
+    __syncwarp();
+    if (lane == 0) x[k] = xk;
+    const T* lk = L + (int64_t)k * m;
+    for (int i = k + 1 + lane; i < m; i += 32) x[i] -= (V)lk[i] * xk;
+    __syncwarp();
+  }
+  for (int k = m - 1; k >= 0; --k) {
+    const T* lk = L + (int64_t)k * m;
+    V s = 0;
+    for (int i = k + 1 + lane; i < m; i += 32) s += (V)lk[i] * x[i];
+    s = warp_sum(s);
+    if (lane == 0) x[k] = (x[k] - s) / (V)L[k + (int64_t)k * m];
+    __syncwarp();
+  }
 }

@@ -7,7 +7,7 @@
 #include "la.cuh"
 
 #ifndef MSDP_SMEM_BYTES
-#define MSDP_SMEM_BYTES (200 * 1024)
+#define MSDP_SMEM_BYTES (72 * 1024)
 #endif
 
 // mixed = 0: FP64 kernel; mixed = 1: FP32 phase + FP64 phase kernel

@@ -17,7 +17,7 @@ enum {
   W_T1, W_T2, W_T3, W_Q, W_DXT, W_DST, W_XT, W_ERD, W_COUNT
 };
 // vectors after the matrices (units of n+1): D, lanczos alpha, beta, w, coef, q
-enum { WV_D = 0, WV_LA, WV_LB, WV_LW, WV_LC, WV_EIG, WV_COUNT };
+enum { WV_D = 0, WV_LA, WV_LB, WV_LW, WV_LC, WV_LA2, WV_LB2, WV_LW2, WV_LC2, WV_EIG, WV_COUNT };
 
 // ---- FP64 vectors of one problem (from ProbDesc::v64)
 // m-vectors
@@ -29,8 +29,17 @@ enum {
   SC_MU = 0, SC_SIGMA, SC_ALPHA, SC_BETA, SC_INFPR, SC_INFDU, SC_GAP, SC_POBJ, SC_DOBJ,
   SC_STATUS, SC_ITER, SC_PHASE, SC_N32, SC_N64, SC_START, SC_SOLVE_NS, SC_BNORM, SC_DNORM,
   SC_CMAX, SC_DC_T, SC_DC_LAM, SC_DC_A, SC_DC_NU, SC_NNEWTON, SC_NPRED, SC_OK, SC_NTRAJ,
-  SC_COUNT = 64
+  // device cycle counters per phase and work counters (profiling)
+  SC_T_CHOL = 32, SC_T_TRTRI, SC_T_JACOBI, SC_T_NTPROD, SC_T_ASSEMBLY, SC_T_FACTOR, SC_T_RHS, SC_T_SOLVE,
+  SC_T_DIRECTIONS, SC_T_STEP, SC_T_LANCZOS, SC_T_CORRECTION, SC_T_TAKE, SC_T_TERM, SC_T_ITER,
+  SC_N_JACOBI_SWEEPS, SC_N_JACOBI_CALLS, SC_N_LANCZOS_STEPS, SC_N_LANCZOS_CALLS, SC_N_FACTOR,
+  SC_PROFILE_END,
+  // the counters above hold the FP32 phase; the FP64 phase uses the same
+  // fields shifted by SC_PROFILE_F64
+  SC_PROFILE_F64 = 24,
+  SC_COUNT = 96
 };
+#define SC_PROFILE_N (SC_PROFILE_END - SC_T_CHOL)
 #define TRAJ_FIELDS 10
 
 // Status value written when the initial point cannot be built (the
@@ -48,8 +57,11 @@ struct ProbDesc {
   int32_t ntraj, pad;
 };
 
+// constraint structure of a block (detected at upload)
+enum { STRUCT_GENERAL = 0, STRUCT_HANKEL = 1 };
+
 struct BlockDesc {
-  int32_t n, pad;
+  int32_t n, structure;
   int64_t nnz;
   int64_t cdat;    // data arena: C (n*n)
   int64_t m64;     // FP64 matrices M_COUNT*n*n + BS_COUNT

@@ -90,6 +90,8 @@ SIGNATURES = [
     ("msdp_batch_get_residuals", i32, [C.c_void_p, i32, P(f64), P(P(f64)), P(f64)]),
     ("msdp_batch_get_block_matrix", i32, [C.c_void_p, i32, i32, i32, P(f64)]),
     ("msdp_batch_launch_count", i64, [C.c_void_p]),
+    ("msdp_batch_get_profile", i32, [C.c_void_p, i32, P(f64), i32]),
+    ("msdp_profile_field_name", C.c_char_p, [i32]),
 ]
 
 _lib = None

@@ -311,6 +311,14 @@ class Batch:
         self.ctx.check(rc, "msdp_batch_get_trajectory")
         return [{k: getattr(arr[i], k) for k, _ in _lib.IterRecord._fields_} for i in range(min(cnt.value, cap))]
 
+    def profile(self, p: int) -> dict:
+        """Device cycle counters per phase and work counters of problem p."""
+        buf = (C.c_double * 128)()
+        n = self.lib.msdp_batch_get_profile(self.h, p, buf, 128)
+        if n < 0:
+            self.ctx.check(n, "msdp_batch_get_profile")
+        return {self.lib.msdp_profile_field_name(i).decode(): buf[i] for i in range(n)}
+
     # --- component-granular steps (identity tests) -------------------------------
     def update_residuals(self):
         self.ctx.check(self.lib.msdp_batch_update_residuals(self.h), "msdp_batch_update_residuals")
