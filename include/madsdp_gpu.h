@@ -66,7 +66,8 @@ enum msdp_error {
   MSDP_ERR_CUDA = -2,
   MSDP_ERR_OUT_OF_MEMORY = -3,
   MSDP_ERR_UNSUPPORTED = -4,      /* combination not built into the kernel */
-  MSDP_ERR_INITIAL_POINT = -5     /* ErrorException of the reference       */
+  MSDP_ERR_INITIAL_POINT = -5,    /* ErrorException of the reference       */
+  MSDP_ERR_TOO_LARGE = -6         /* beyond the limits of msdp_solve_static */
 };
 
 /* Components: mirror src/components.jl:30-300 with their default values. */
@@ -209,6 +210,36 @@ enum msdp_block_matrix { MSDP_MAT_W = 0, MSDP_MAT_CORR = 1, MSDP_MAT_SI = 2, MSD
  * msdp_profile_field_name); returns the number of fields written. */
 int msdp_batch_get_profile(msdp_batch* batch, int32_t prob, double* out, int32_t capacity);
 const char* msdp_profile_field_name(int32_t index);
+
+/* ---- solve without allocating --------------------------------------------
+ * msdp_solve_static has no counterpart in the reference.  It is for callers
+ * that may not allocate device memory: a serving runtime or plugin host that
+ * owns every byte of the GPU through its own pool, or a control loop that
+ * must not pay for (or risk failing) a cudaMalloc/cudaFree.  It solves ONE
+ * problem with the FP64 kernel of msdp_batch_solve, but every device-side
+ * buffer lives in one static device array of MSDP_STATIC_SCRATCH_BYTES that
+ * each GPU loading the library holds until exit.  It issues only
+ * cudaMemcpyAsync, cudaMemsetAsync and kernel launches on `stream` (a
+ * cudaStream_t; NULL = default stream) and waits for them; it calls no
+ * cudaMalloc, cudaFree or allocating library routine.  Inputs are the host
+ * problem description; outputs are written to the caller's host buffers
+ * (X per block, y, x, z and stats; NULL pointers are skipped).
+ *
+ * Limits: at most MSDP_STATIC_MAX_BLOCKS blocks and a total layout (problem
+ * data, constraint lists and workspaces) that fits the array, roughly
+ * sum_i 250 n_i^2 + 8 m^2 + 52 nnz bytes; larger problems return
+ * MSDP_ERR_TOO_LARGE.  PrimalDual + DenseCholesky in FP64 with ScaledIdentity
+ * or DualShift only (MSDP_ERR_UNSUPPORTED otherwise).
+ *
+ * The first call on a device looks up the array's device address with
+ * cudaGetSymbolAddress (with that device current); make that first call
+ * before any stream capture.  Every call reuses the same array and zeroes it
+ * before use, so calls that overlap on the GPU (other threads, other streams)
+ * race and must be serialized by the caller. */
+#define MSDP_STATIC_SCRATCH_BYTES (16ll * 1024 * 1024)
+#define MSDP_STATIC_MAX_BLOCKS 16
+int msdp_solve_static(const msdp_problem_desc* problem, const msdp_components* comp, const msdp_options* opt,
+                      void* stream, double* const* X, double* y, double* x, double* z, msdp_stats* stats);
 
 /* Number of kernel launches issued by this batch since creation. */
 int64_t msdp_batch_launch_count(const msdp_batch* batch);

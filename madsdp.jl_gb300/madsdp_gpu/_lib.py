@@ -92,6 +92,8 @@ SIGNATURES = [
     ("msdp_batch_launch_count", i64, [C.c_void_p]),
     ("msdp_batch_get_profile", i32, [C.c_void_p, i32, P(f64), i32]),
     ("msdp_profile_field_name", C.c_char_p, [i32]),
+    ("msdp_solve_static", i32, [P(ProblemDesc), P(Components), P(Options), C.c_void_p, P(P(f64)), P(f64),
+                                P(f64), P(f64), P(Stats)]),
 ]
 
 _lib = None
@@ -115,4 +117,5 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     return lib
 
 
-ERRORS = {0: "OK", -1: "INVALID_ARGUMENT", -2: "CUDA", -3: "OUT_OF_MEMORY", -4: "UNSUPPORTED", -5: "INITIAL_POINT"}
+ERRORS = {0: "OK", -1: "INVALID_ARGUMENT", -2: "CUDA", -3: "OUT_OF_MEMORY", -4: "UNSUPPORTED", -5: "INITIAL_POINT",
+          -6: "TOO_LARGE"}
