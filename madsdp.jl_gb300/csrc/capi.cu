@@ -172,8 +172,16 @@ int msdp_batch_create(msdp_context* ctx, const msdp_problem_desc* probs, int32_t
   // ---- component checks (src/qr_schur.jl:12-22, src/dual_centering.jl:68-76)
   if (c.schur == MSDP_QR_SCHUR && !(c.algorithm == MSDP_PRIMAL_DUAL && c.direction == MSDP_NT))
     return fail(ctx, MSDP_ERR_INVALID_ARGUMENT, "QRSchur requires PrimalDual with the NT direction.");
-  if (c.algorithm != MSDP_PRIMAL_DUAL)
-    return fail(ctx, MSDP_ERR_UNSUPPORTED, "DualCentering is not built into the device kernel");
+  if (c.algorithm == MSDP_DUAL_CENTERING) {
+    for (int p = 0; p < nprob; ++p) {
+      if (probs[p].ns > 0)
+        return fail(ctx, MSDP_ERR_INITIAL_POINT, "MadSDP: `DualCentering` does not support scalar (LP) blocks yet.");
+      if (probs[p].nblocks == 0)
+        return fail(ctx, MSDP_ERR_INITIAL_POINT, "MadSDP: `DualCentering` needs at least one PSD block.");
+    }
+  } else if (c.algorithm != MSDP_PRIMAL_DUAL) {
+    return fail(ctx, MSDP_ERR_INVALID_ARGUMENT, "unknown algorithm");
+  }
   if (c.schur != MSDP_DENSE_CHOLESKY)
     return fail(ctx, MSDP_ERR_UNSUPPORTED, "only the DenseCholesky Schur solver is built into the device kernel");
   if (c.initial_point == MSDP_SCALED_IDENTITY && c.scale != 0.0 && !(std::isfinite(c.scale) && c.scale > 0.0))

@@ -1092,6 +1092,250 @@ struct Algo {
   __device__ bool iterate_pd(bool strict) {
     return prm.centering == MSDP_MEHROTRA ? iterate_mehrotra(strict) : iterate_adaptive(strict);
   }
+
+  // ================================================================ DualCentering
+  // src/dual_centering.jl: the method carries y, S = C - A*(y) (always
+  // feasible) and t; X is an estimate after each predictor step.
+
+  // S = C - A*(y), factor and invert every block (:83-86)
+  __noinline__ __device__ bool refresh_slacks() {
+    set_dual_slacks();
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      if (!chol_factor<T, double>(b.n, b.S, b.W(W_LS), true, smem, sh)) return false;
+      tri_inverse<T>(b.n, b.W(W_LS), b.W(W_LSI), smem);
+      cta_gemm<T>(b.n, 1, 0, 1, 1, (T)1, b.W(W_LSI), b.W(W_LSI), (T)0, b.W(W_SI), scr());
+      cta_symmetrize<T>(b.n, b.W(W_SI));
+    }
+    return true;
+  }
+
+  // g = A(S^-1) - t b (:89-98); d = H^-1 g, lambda = sqrt(g'd) (:102-110)
+  __noinline__ __device__ bool newton_direction() {
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.dcgz[j] = 0.0;
+    __syncthreads();
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      jprod_add(b, P.m, b.W(W_SI), P.dcgz);
+    }
+    const double t = P.sc[SC_DC_T];
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.dcg[j] = P.dcgz[j] - t * P.b[j];
+    __syncthreads();
+    if (!factorize_schur()) return false;
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.dcd[j] = P.dcg[j];
+    __syncthreads();
+    schur_solve(P.dcd);
+    double gd = 0.0;
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) gd = fma(P.dcg[j], P.dcd[j], gd);
+    gd = block_sum(gd, &sh.rb);
+    if (threadIdx.x == 0) P.sc[SC_DC_LAM] = sqrt(fmax(gd, 0.0));
+    __syncthreads();
+    return true;
+  }
+
+  // y -= d / (1 + lambda)
+  __device__ void damped_newton_step() {
+    const double lam = P.sc[SC_DC_LAM];
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.y[j] -= P.dcd[j] / (1.0 + lam);
+    __syncthreads();
+  }
+
+  // initialize_algorithm!(solver, ::DualCentering) (:112-143); returns
+  // false where the reference throws ErrorException.
+  __noinline__ __device__ bool dc_initialize() {
+    const double beta = prm.dc_beta;
+    if (threadIdx.x == 0) {
+      P.sc[SC_DC_NU] = (double)(nu() - P.ns);
+      if (isnan(prm.dc_A)) {
+        const double tau = 2.0 * beta / ((1.0 - beta) * (1.0 - beta));
+        P.sc[SC_DC_A] = prm.dc_delta + (-tau - log1p(-tau));
+      } else {
+        P.sc[SC_DC_A] = prm.dc_A;
+      }
+      P.sc[SC_NNEWTON] = 0.0;
+      P.sc[SC_NPRED] = 0.0;
+      P.sc[SC_DC_T] = 0.0;
+    }
+    __syncthreads();
+    if (!refresh_slacks()) return false;
+    if (!newton_direction()) return false;
+    // d = B grad(zeta) (t = 0) and dy = B b
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.dcdy[j] = P.b[j];
+    __syncthreads();
+    schur_solve(P.dcdy);
+    double bBb = 0.0, bBg = 0.0;
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) {
+      bBb = fma(P.b[j], P.dcdy[j], bBb);
+      bBg = fma(P.b[j], P.dcd[j], bBg);
+    }
+    bBb = fmax(block_sum(bBb, &sh.rb), 2.220446049250313e-16);
+    bBg = block_sum(bBg, &sh.rb);
+    if (threadIdx.x == 0) P.sc[SC_DC_T] = fmax(bBg / bBb, beta / sqrt(bBb));
+    __syncthreads();
+    for (int it = 0; it < prm.centering_max_iter; ++it) {
+      if (!newton_direction()) return false;
+      if (P.sc[SC_DC_LAM] <= beta / 2) break;
+      damped_newton_step();
+      if (threadIdx.x == 0) { P.sc[SC_ITER] += 1.0; P.sc[SC_NNEWTON] += 1.0; }
+      __syncthreads();
+      if (!refresh_slacks()) return false;
+    }
+    if (threadIdx.x == 0) P.sc[SC_MU] = 1.0 / P.sc[SC_DC_T];
+    __syncthreads();
+    return true;
+  }
+
+  // xi(alpha) = sum -log(1 - alpha mu) - log(1 + alpha/(1-alpha) mu) over the
+  // proximity eigenvalues of every block (:146-160); one warp.
+  __device__ double xi_value(double alpha) {
+    const int lane = threadIdx.x & 31;
+    double s = 0.0;
+    int bad = 0;
+    const double b2 = alpha / (1.0 - alpha);
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const T* ev = b.V(WV_EIG);
+      for (int k = lane; k < b.n; k += 32) {
+        const double mu = (double)ev[k];
+        const double u = 1.0 - alpha * mu, v = 1.0 + b2 * mu;
+        if (!(u > 0.0 && v > 0.0)) bad = 1;
+        else s -= log(u) + log(v);
+      }
+    }
+    s = warp_sum(s);
+    bad = __any_sync(0xffffffffu, bad);
+    return bad ? INFINITY : s;
+  }
+
+  // bisection on xi(alpha) = A (:163-201); one warp
+  __device__ double solve_alpha(double A) {
+    const int lane = threadIdx.x & 31;
+    double amax = 1.0;
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const T* ev = b.V(WV_EIG);
+      for (int k = lane; k < b.n; k += 32) {
+        const double mu = (double)ev[k];
+        if (mu > 0.0) amax = fmin(amax, 1.0 / mu);
+        if (mu < 0.0) amax = fmin(amax, 1.0 / (1.0 - mu));
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) amax = fmin(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    double hi = amax * 0.99999;
+    const double xhi = xi_value(hi);
+    if (!isfinite(xhi) || xhi < A) return hi;
+    double lo = 0.0;
+    for (int it = 0; it < 80; ++it) {
+      const double mid = (lo + hi) / 2;
+      if (xi_value(mid) < A) lo = mid;
+      else hi = mid;
+      if (hi - lo <= 2.220446049250313e-16 * fmax(1.0, hi)) break;
+    }
+    return (lo + hi) / 2;
+  }
+
+  // _predictor_step! (:232-264)
+  __noinline__ __device__ bool predictor_step() {
+    const double t = P.sc[SC_DC_T];
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) {
+      P.dcyhat[j] = P.y[j] + P.dcd[j];
+      P.dcdy[j] = P.b[j];
+    }
+    __syncthreads();
+    schur_solve(P.dcdy);
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.dcdy[j] *= t;
+    __syncthreads();
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const int n = b.n;
+      slack(b, P.dcyhat, b.Shat);                       // S_hat = sym(C - A*(y_hat))
+      jtprod_combine(b, P.dcdy, 1.0, nullptr, nullptr, b.Dc);
+      cta_symmetrize<double>(n, b.Dc);                  // D = sym(A*(dy))
+      // eigenvalues of L_hat^-1 D L_hat^-T (:205-215)
+      if (!chol_factor<T, double>(n, b.Shat, b.W(W_LX), true, smem, sh)) return false;
+      tri_inverse<T>(n, b.W(W_LX), b.W(W_LXI), smem);
+      T* dt = as_T<T>(b.nn, b.Dc, b.W(W_DXT));
+      cta_gemm<T>(n, 0, 0, 1, 0, (T)1, b.W(W_LXI), dt, (T)0, b.W(W_T1), scr());
+      cta_gemm<T>(n, 0, 1, 0, 1, (T)1, b.W(W_T1), b.W(W_LXI), (T)0, b.W(W_T2), scr());
+      cta_symmetrize<T>(n, b.W(W_T2));
+      if ((threadIdx.x >> 5) == 0)
+        warp_lanczos_full<T>(n, b.W(W_T2), b.W(W_Q), b.V(WV_LA), b.V(WV_LB), b.V(WV_LW), b.V(WV_LC));
+      __syncthreads();
+      T* ev = b.V(WV_EIG);
+      for (int k = threadIdx.x; k < n; k += NTHREADS) ev[k] = thread_tridiag_eig<T>(n, b.V(WV_LA), b.V(WV_LB), k);
+      __syncthreads();
+    }
+    // ||s_hat||^2 = sum ||Ls^-1 S_hat Ls^-T||_F^2 (:219-229)
+    double shat_n2 = 0.0;
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      T* st = as_T<T>(b.nn, b.Shat, b.W(W_DST));
+      cta_gemm<T>(b.n, 0, 0, 1, 0, (T)1, b.W(W_LSI), st, (T)0, b.W(W_T1), scr());
+      cta_gemm<T>(b.n, 0, 1, 0, 1, (T)1, b.W(W_T1), b.W(W_LSI), (T)0, b.W(W_T2), scr());
+      const T* z = b.W(W_T2);
+      double s2 = 0.0;
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) s2 = fma((double)z[k], (double)z[k], s2);
+      shat_n2 += block_sum(s2, &sh.rb);
+    }
+    if ((threadIdx.x >> 5) == 0) {
+      const double alpha = solve_alpha(P.sc[SC_DC_A]);
+      if (threadIdx.x == 0) sh.bc[6] = alpha;
+    }
+    __syncthreads();
+    const double alpha = sh.bc[6];
+    __syncthreads();
+    if (threadIdx.x == 0) { P.sc[SC_ALPHA] = alpha; P.sc[SC_BETA] = alpha; }
+    // primal estimate X = (1/t) S^-1 ((1-alpha) S_hat + alpha D) S^-1
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      T* buf = b.W(W_T3);
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) buf[k] = (T)((1.0 - alpha) * b.Shat[k] + alpha * b.Dc[k]);
+      __syncthreads();
+      cta_gemm<T>(b.n, 0, 0, 0, 0, (T)1, b.W(W_SI), buf, (T)0, b.W(W_T1), scr());
+      cta_gemm<T>(b.n, 0, 0, 0, 0, (T)(1.0 / t), b.W(W_T1), b.W(W_SI), (T)0, b.W(W_T2), scr());
+      const T* xt = b.W(W_T2);
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) b.X[k] = (double)xt[k];
+      __syncthreads();
+      cta_symmetrize<double>(b.n, b.X);
+    }
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.y[j] = P.dcyhat[j] + alpha * P.dcdy[j];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      P.sc[SC_DC_T] = P.sc[SC_DC_NU] * t / ((1.0 - alpha) * shat_n2);
+      P.sc[SC_NPRED] += 1.0;
+    }
+    __syncthreads();
+    return true;
+  }
+
+  // iterate!(solver, ::DualCentering) (:266-289)
+  __noinline__ __device__ void dc_iterate() {
+    bool ok = newton_direction();
+    if (ok) {
+      const double lam = P.sc[SC_DC_LAM];
+      if (lam > prm.dc_beta) {
+        damped_newton_step();
+        if (threadIdx.x == 0) {
+          P.sc[SC_ALPHA] = P.sc[SC_BETA] = 1.0 / (1.0 + lam);
+          P.sc[SC_NNEWTON] += 1.0;
+        }
+        __syncthreads();
+      } else {
+        ok = predictor_step();
+      }
+    }
+    if (ok) {
+      if (threadIdx.x == 0) P.sc[SC_ITER] += 1.0;
+      __syncthreads();
+      ok = refresh_slacks();
+    }
+    if (threadIdx.x == 0) {
+      if (!ok) P.sc[SC_STATUS] = (double)MSDP_ERROR_IN_STEP_COMPUTATION;
+      else P.sc[SC_MU] = 1.0 / P.sc[SC_DC_T];
+    }
+    __syncthreads();
+  }
 };
 
 template <> __device__ __forceinline__ const double* Algo<double>::xt(const Blk<double>& b) const { return b.X; }

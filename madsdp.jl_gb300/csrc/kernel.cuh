@@ -14,6 +14,7 @@ namespace {
 __device__ void update_termination(const BatchDev& B, Prob& P, unsigned char* smem, SharedState& sh) {
   Algo<double> A(B, P, smem, sh);
   const Params& prm = B.prm;
+  if (prm.algorithm == MSDP_DUAL_CENTERING) A.update_residuals();
   double pobj = 0.0, rdmax = 0.0;
   for (int i = 0; i < P.nblocks; ++i) {
     Blk<double> b = A.blk(i);
@@ -153,6 +154,7 @@ __device__ bool initialize(const BatchDev& B, Prob& P, unsigned char* smem, Shar
     for (int k = SC_T_CHOL; k < SC_PROFILE_END; ++k) { P.sc[k] = 0.0; P.sc[k + SC_PROFILE_F64] = 0.0; }
   }
   __syncthreads();
+  if (prm.algorithm == MSDP_DUAL_CENTERING) return A.dc_initialize();
   // initialize_algorithm!(solver, ::PrimalDual)
   A.update_residuals();
   const double mu = A.total_complementarity() / fmax((double)nu, 1.0);
@@ -166,6 +168,11 @@ __device__ bool initialize(const BatchDev& B, Prob& P, unsigned char* smem, Shar
 template <int MIXED>
 __device__ void iterate_one(const BatchDev& B, Prob& P, unsigned char* smem, SharedState& sh) {
   const Params& prm = B.prm;
+  if (prm.algorithm == MSDP_DUAL_CENTERING) {
+    Algo<double> A(B, P, smem, sh);
+    A.dc_iterate();
+    return;
+  }
   if constexpr (MIXED != 0) {
     int phase = (int)P.sc[SC_PHASE];
     if (phase == 0 && fmax(fmax(P.sc[SC_INFPR], P.sc[SC_INFDU]), P.sc[SC_GAP]) < prm.switch_tol) phase = 1;

@@ -622,3 +622,97 @@ __device__ void warp_potrs(int m, const T* __restrict__ L, V* x) {
     __syncwarp();
   }
 }
+
+// Full Lanczos tridiagonalization of the symmetric Z (n x n) by ONE warp:
+// n steps with full reorthogonalization; when the Krylov space closes early
+// (b ~ 0) it restarts from a new vector orthogonal to the basis (b = 0 in
+// T), so T (a[0..n), bb[1..n)) has exactly the eigenvalues of Z.
+template <class T>
+__device__ void warp_lanczos_full(int n, const T* Z, T* Q, T* a, T* bb, T* w, T* coef) {
+  const int lane = threadIdx.x & 31;
+  auto start_vector = [&](int j, uint32_t seed) {
+    T* q = Q + (int64_t)j * n;
+    for (int i = lane; i < n; i += 32) {
+      uint32_t h = (uint32_t)(i + 1) * 2654435761u + seed * 40503u;
+      h ^= h >> 15; h *= 2246822519u; h ^= h >> 13;
+      q[i] = (T)((double)(h & 0xffffff) / 16777216.0 - 0.5) + (T)0.01;
+    }
+    __syncwarp();
+    // orthogonalize twice against the previous columns, then normalize
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int l = lane; l < j; l += 32) {
+        const T* ql = Q + (int64_t)l * n;
+        T s = 0;
+        for (int i = 0; i < n; ++i) s = fma(ql[i], q[i], s);
+        coef[l] = s;
+      }
+      __syncwarp();
+      for (int i = lane; i < n; i += 32) {
+        T v = q[i];
+        for (int l = 0; l < j; ++l) v = fma(-coef[l], Q[i + (int64_t)l * n], v);
+        q[i] = v;
+      }
+      __syncwarp();
+    }
+    T nrm = 0;
+    for (int i = lane; i < n; i += 32) nrm = fma(q[i], q[i], nrm);
+    nrm = Num<T>::sqrt_(warp_sum(nrm));
+    const T inv = nrm > (T)0 ? (T)1 / nrm : (T)0;
+    for (int i = lane; i < n; i += 32) q[i] *= inv;
+    __syncwarp();
+  };
+  start_vector(0, 1u);
+  T znorm = 0;
+  for (int j = 0; j < n; ++j) {
+    const T* qj = Q + (int64_t)j * n;
+    for (int i = lane; i < n; i += 32) {
+      T s = 0;
+      for (int r = 0; r < n; ++r) s = fma(Z[i + (int64_t)r * n], qj[r], s);
+      w[i] = s;
+    }
+    __syncwarp();
+    T aj = 0;
+    for (int i = lane; i < n; i += 32) aj = fma(qj[i], w[i], aj);
+    aj = warp_sum(aj);
+    const T bj = j > 0 ? bb[j] : (T)0;
+    const T* qp = j > 0 ? Q + (int64_t)(j - 1) * n : qj;
+    for (int i = lane; i < n; i += 32) {
+      T v = w[i] - aj * qj[i];
+      if (j > 0) v -= bj * qp[i];
+      w[i] = v;
+    }
+    if (lane == 0) a[j] = aj;
+    __syncwarp();
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int l = lane; l <= j; l += 32) {
+        const T* ql = Q + (int64_t)l * n;
+        T s = 0;
+        for (int i = 0; i < n; ++i) s = fma(ql[i], w[i], s);
+        coef[l] = s;
+      }
+      __syncwarp();
+      for (int i = lane; i < n; i += 32) {
+        T v = w[i];
+        for (int l = 0; l <= j; ++l) v = fma(-coef[l], Q[i + (int64_t)l * n], v);
+        w[i] = v;
+      }
+      __syncwarp();
+    }
+    if (j + 1 == n) break;
+    T bn = 0;
+    for (int i = lane; i < n; i += 32) bn = fma(w[i], w[i], bn);
+    bn = Num<T>::sqrt_(warp_sum(bn));
+    znorm = fmax(znorm, fabs(aj) + bn + fabs(bj));
+    T* qn = Q + (int64_t)(j + 1) * n;
+    if (bn > Num<T>::eps() * fmax(znorm, (T)1e-300) * (T)4) {
+      const T inv = (T)1 / bn;
+      for (int i = lane; i < n; i += 32) qn[i] = w[i] * inv;
+      if (lane == 0) bb[j + 1] = bn;
+      __syncwarp();
+    } else {
+      if (lane == 0) bb[j + 1] = (T)0;
+      __syncwarp();
+      start_vector(j + 1, (uint32_t)(j + 2));
+    }
+  }
+}

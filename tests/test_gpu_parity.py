@@ -212,3 +212,54 @@ def test_batch_uneven_results_independent_of_mix(gpu_ctx):
         assert a["status"] == st_all[i]["status"] == M.Status.SOLVE_SUCCEEDED
         assert a["iter"] == st_all[i]["iter"]
         assert a["pobj"] == st_all[i]["pobj"] and a["dobj"] == st_all[i]["dobj"]
+
+
+# ------------------------------------------------------------------ DualCentering
+@pytest.mark.parametrize("case", KA["dual_centering"], ids=lambda c: c["model"])
+def test_dual_centering_known_answers(gpu_ctx, case):
+    s = gpu_solve(build(case["model"]), algorithm=M.DualCentering(), tol=case["tol"], max_iter=case["max_iter"])
+    assert s.status == M.Status.SOLVE_SUCCEEDED, s.stats
+    assert abs(s.dual_objective() - case["dual_objective"]) <= case["atol"]
+    if "primal_objective" in case:
+        assert abs(s.primal_objective() - case["primal_objective"]) <= case["atol"]
+    if "inf_du_below" in case:
+        assert s.inf_du < case["inf_du_below"]
+    ref = o.Solver(build(case["model"]), algorithm=o.DualCentering(), tol=case["tol"], max_iter=case["max_iter"]).solve()
+    assert abs(s.iter - ref.iter) <= 1
+    scale = max(1.0, abs(ref.dual_objective()))
+    assert abs(s.dual_objective() - ref.dual_objective()) <= 1e-7 * scale
+    st = s.stats
+    assert st["n_newton"] == ref.n_newton and st["n_predictor"] == ref.n_predictor
+
+
+def test_dual_centering_theoretical_A(gpu_ctx):
+    # test/dual_runtests.jl:76-101 (second half; DenseCholesky on the device)
+    L = laplacian(g.weighted_4node_W())
+    y0 = -(1 + np.abs(L / 4).sum(axis=0))
+    s = gpu_solve(build("maxcut_weighted4"), algorithm=M.DualCentering(A=None),
+                  initial_point=M.InitialPoint([np.eye(4)], y0), tol=1e-6, max_iter=300)
+    assert s.status == M.Status.SOLVE_SUCCEEDED
+    assert abs(s.dual_objective() + 18.0) <= 1e-3
+
+
+def test_dual_centering_errors(gpu_ctx):
+    # test/dual_runtests.jl:103-131
+    model = g.maxcut_from_weights(np.ones((2, 2)) - np.eye(2))
+    with pytest.raises(RuntimeError):
+        gpu_solve(model, algorithm=M.DualCentering(),
+                  initial_point=M.InitialPoint([np.eye(2)], np.array([1.0, 1.0])))
+    with pytest.raises(RuntimeError):
+        gpu_solve(model, algorithm=M.DualCentering(), initial_point=M.DualShift(1.0, 0.1))
+    with pytest.raises(RuntimeError):
+        M.MadSDPSolver(build("mixed_lp"), algorithm=M.DualCentering())
+
+
+def test_dual_centering_trajectory(gpu_ctx):
+    model = g.maxcut(20, 0.3, seed=8)
+    ref = o.Solver(model, algorithm=o.DualCentering()).solve()
+    s = gpu_solve(model, algorithm=M.DualCentering())
+    assert s.status == M.Status.SOLVE_SUCCEEDED
+    assert abs(s.iter - ref.iter) <= 1
+    compare_trajectories(s.trajectory(), ref.trajectory)
+    st = s.stats
+    assert st["n_newton"] > 0 and st["n_predictor"] > 0
