@@ -61,6 +61,8 @@ struct Prob {
   float *Hf, *Lf;
   double* traj;
   int ntraj;
+  int K;
+  double *qrB, *qrtau, *qrscale, *qrbase, *qrdir;
 };
 
 __device__ __forceinline__ Prob make_prob(const BatchDev& B, int p) {
@@ -89,6 +91,16 @@ __device__ __forceinline__ Prob make_prob(const BatchDev& B, int p) {
   P.Lf = d.Lf >= 0 ? B.d32 + d.Lf : nullptr;
   P.traj = B.d64 + d.traj;
   P.ntraj = d.ntraj;
+  P.K = d.K;
+  if (d.qr >= 0) {
+    P.qrB = B.d64 + d.qr;
+    P.qrtau = P.qrB + (int64_t)d.K * m;
+    P.qrscale = P.qrtau + m;
+    P.qrbase = P.qrscale + m;
+    P.qrdir = P.qrbase + d.K;
+  } else {
+    P.qrB = P.qrtau = P.qrscale = P.qrbase = P.qrdir = nullptr;
+  }
   return P;
 }
 
@@ -663,6 +675,7 @@ struct Algo {
 
   // factorize_schur! with the regularization retry loop (src/solver.jl:299-314)
   __noinline__ __device__ bool factorize_schur() {
+    if (prm.schur == MSDP_QR_SCHUR) return qr_factorize();
     const int m = P.m;
     const int64_t mm = (int64_t)m * m;
     T* H = schur_H();
@@ -1021,6 +1034,10 @@ struct Algo {
   }
 
   __noinline__ __device__ void solve_directions(double mu, bool corrected) {
+    if (prm.schur == MSDP_QR_SCHUR) {
+      qr_solve_directions(mu, corrected);
+      return;
+    }
     PROF_BEGIN(r);
     rhs(mu, corrected);
     for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.dely[j] = P.h[j];
@@ -1091,6 +1108,224 @@ struct Algo {
 
   __device__ bool iterate_pd(bool strict) {
     return prm.centering == MSDP_MEHROTRA ? iterate_mehrotra(strict) : iterate_adaptive(strict);
+  }
+
+  // ================================================================ QRSchur
+  // src/qr_schur.jl: B[:, j] = svec(G' A_j G) (off-diagonals times sqrt 2)
+  // over the blocks, then sqrt(x/z) C_lin' for the scalars; columns are
+  // equilibrated and B D = Q R by Householder reflections (dense QR in
+  // place of SPQR; the projection solve does not depend on the ordering).
+
+  // svec position of (p, q), p <= q, column-major upper triangle
+  __device__ __forceinline__ static int64_t svec_index(int p, int q) { return (int64_t)q * (q + 1) / 2 + p; }
+
+  __noinline__ __device__ bool qr_factorize() {
+    const int m = P.m, K = P.K;
+    double* B = P.qrB;
+    // ---- assemble B
+    int64_t off = 0;
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const int n = b.n;
+      const int64_t nv = (int64_t)n * (n + 1) / 2;
+      const T* G = b.W(W_G);
+      for (int j = 0; j < m; ++j) {
+        const int64_t e0 = b.cptr[j], e1 = b.cptr[j + 1];
+        double* col = B + (int64_t)j * K + off;
+        for (int64_t t = threadIdx.x; t < nv; t += NTHREADS) {
+          int q = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+          while ((int64_t)(q + 1) * (q + 2) / 2 <= t) ++q;
+          while ((int64_t)q * (q + 1) / 2 > t) --q;
+          const int p = (int)(t - (int64_t)q * (q + 1) / 2);
+          double v = 0.0;
+          for (int64_t e = e0; e < e1; ++e)
+            v = fma(b.eval[e] * (double)G[b.erow[e] + (int64_t)p * n], (double)G[b.ecol[e] + (int64_t)q * n], v);
+          col[t] = (p == q) ? v : v * 1.4142135623730951;
+        }
+      }
+      off += nv;
+    }
+    for (int k = threadIdx.x; k < P.ns; k += NTHREADS) {
+      const double w = sqrt(P.x[k] / P.z[k]);
+      for (int j = 0; j < m; ++j) B[(int64_t)j * K + off + k] = w * P.Clin[j + (int64_t)k * m];
+    }
+    __syncthreads();
+    // ---- column equilibration (src/qr_schur.jl:73-82)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int bad = 0;
+    for (int j = warp; j < m; j += NWARPS) {
+      const double* col = B + (int64_t)j * K;
+      double s = 0.0;
+      for (int t = lane; t < K; t += 32) s = fma(col[t], col[t], s);
+      s = sqrt(warp_sum(s));
+      if (lane == 0) {
+        if (s == 0.0 || !isfinite(s)) bad = 1;
+        else P.qrscale[j] = 1.0 / s;
+      }
+    }
+    bad = __syncthreads_or(bad);
+    if (bad || K < m) return false;
+    for (int64_t t = threadIdx.x; t < (int64_t)K * m; t += NTHREADS) B[t] *= P.qrscale[t / K];
+    __syncthreads();
+    // ---- Householder QR, reflectors below the diagonal, R above (dgeqr2)
+    for (int k = 0; k < m; ++k) {
+      double* bk = B + (int64_t)k * K;
+      double s = 0.0;
+      for (int i = k + 1 + threadIdx.x; i < K; i += NTHREADS) s = fma(bk[i], bk[i], s);
+      s = block_sum(s, &sh.rb);
+      const double a0 = bk[k];
+      double tau = 0.0;
+      if (s != 0.0) {
+        const double beta = -copysign(sqrt(a0 * a0 + s), a0);
+        tau = (beta - a0) / beta;
+        const double scal = 1.0 / (a0 - beta);
+        for (int i = k + 1 + threadIdx.x; i < K; i += NTHREADS) bk[i] *= scal;
+        __syncthreads();
+        if (threadIdx.x == 0) bk[k] = beta;
+      }
+      if (threadIdx.x == 0) P.qrtau[k] = tau;
+      __syncthreads();
+      if (tau != 0.0) {
+        for (int c = k + 1 + warp; c < m; c += NWARPS) {
+          double* bc = B + (int64_t)c * K;
+          double w = 0.0;
+          for (int i = k + 1 + lane; i < K; i += 32) w = fma(bk[i], bc[i], w);
+          w = warp_sum(w) + bc[k];
+          const double tw = tau * w;
+          if (lane == 0) bc[k] -= tw;
+          for (int i = k + 1 + lane; i < K; i += 32) bc[i] = fma(-tw, bk[i], bc[i]);
+        }
+        __syncthreads();
+      }
+    }
+    // rank test: every R_ii nonzero (src/qr_schur.jl:86-87)
+    int zero = 0;
+    for (int k = threadIdx.x; k < m; k += NTHREADS) zero |= (B[(int64_t)k * K + k] == 0.0);
+    zero = __syncthreads_or(zero);
+    return !zero;
+  }
+
+  // u <- H_k u for k = first..last (step +1 or -1); u length K
+  __device__ void qr_apply(double* u, bool transpose) {
+    const int m = P.m, K = P.K;
+    const double* B = P.qrB;
+    for (int it = 0; it < m; ++it) {
+      const int k = transpose ? it : m - 1 - it;
+      const double tau = P.qrtau[k];
+      if (tau == 0.0) continue;
+      const double* bk = B + (int64_t)k * K;
+      double w = 0.0;
+      for (int i = k + 1 + threadIdx.x; i < K; i += NTHREADS) w = fma(bk[i], u[i], w);
+      w = block_sum(w, &sh.rb) + u[k];
+      const double tw = tau * w;
+      for (int i = k + 1 + threadIdx.x; i < K; i += NTHREADS) u[i] = fma(-tw, bk[i], u[i]);
+      if (threadIdx.x == 0) u[k] -= tw;
+      __syncthreads();
+    }
+  }
+
+  // solve_directions!(::QRSchurWorkspace, ...) (src/qr_schur.jl:90-160)
+  __noinline__ __device__ void qr_solve_directions(double mu, bool corrected) {
+    const int m = P.m, K = P.K;
+    const double* B = P.qrB;
+    double* base = P.qrbase;
+    double* u = P.qrdir;
+    int64_t off = 0;
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const int n = b.n;
+      const int64_t nv = (int64_t)n * (n + 1) / 2;
+      // T = -G' Rd G + diag(mu / D - D) (+ RNT)
+      T* rdt = as_T<T>(b.nn, b.Rd, b.W(W_T3));
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, rdt, b.W(W_G), (T)0, b.W(W_T1), scr());
+      cta_gemm<T>(n, 1, 0, 0, 0, (T)-1, b.W(W_G), b.W(W_T1), (T)0, b.W(W_T2), scr());
+      const T* Tm = b.W(W_T2);
+      const T* D = b.V(WV_D);
+      const T* RNT = b.W(W_RNT);
+      for (int64_t t = threadIdx.x; t < nv; t += NTHREADS) {
+        int q = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+        while ((int64_t)(q + 1) * (q + 2) / 2 <= t) ++q;
+        while ((int64_t)q * (q + 1) / 2 > t) --q;
+        const int p = (int)(t - (int64_t)q * (q + 1) / 2);
+        double v = (double)Tm[p + (int64_t)q * n];
+        if (p == q) v += mu / (double)D[p] - (double)D[p];
+        if (corrected) v += (double)RNT[p + (int64_t)q * n];
+        base[off + t] = (p == q) ? v : 1.4142135623730951 * v;
+      }
+      __syncthreads();
+      off += nv;
+    }
+    for (int k = threadIdx.x; k < P.ns; k += NTHREADS) {
+      const double w = sqrt(P.x[k] / P.z[k]), prod = sqrt(P.x[k] * P.z[k]);
+      double v = mu / prod - prod - w * P.Rdlin[k];
+      if (corrected) v += P.corrlin[k] / w;
+      base[off + k] = v;
+    }
+    __syncthreads();
+    // qbase = Q' base
+    for (int t = threadIdx.x; t < K; t += NTHREADS) u[t] = base[t];
+    __syncthreads();
+    qr_apply(u, true);
+    // c = R^-T (scale .* Rp); t = c - qbase[0:m]  (one warp, forward substitution)
+    double* cvec = P.wm;
+    double* dy = P.dely;
+    if ((threadIdx.x >> 5) == 0) {
+      const int lane = threadIdx.x & 31;
+      for (int j = 0; j < m; ++j) {
+        double s = 0.0;
+        for (int l = lane; l < j; l += 32) s = fma(B[l + (int64_t)j * K], cvec[l], s);
+        s = warp_sum(s);
+        if (lane == 0) cvec[j] = (P.qrscale[j] * P.Rp[j] - s) / B[j + (int64_t)j * K];
+        __syncwarp();
+      }
+      for (int j = lane; j < m; j += 32) cvec[j] -= u[j];
+      __syncwarp();
+      // dy = scale .* (R^-1 t)  (back substitution)
+      for (int j = m - 1; j >= 0; --j) {
+        double s = 0.0;
+        for (int l = j + 1 + lane; l < m; l += 32) s = fma(B[j + (int64_t)l * K], dy[l], s);
+        s = warp_sum(s);
+        if (lane == 0) dy[j] = (cvec[j] - s) / B[j + (int64_t)j * K];
+        __syncwarp();
+      }
+      for (int j = lane; j < m; j += 32) dy[j] *= P.qrscale[j];
+    }
+    __syncthreads();
+    // direction = base + Q [t; 0]
+    for (int t = threadIdx.x; t < K; t += NTHREADS) u[t] = t < m ? cvec[t] : 0.0;
+    __syncthreads();
+    qr_apply(u, false);
+    for (int t = threadIdx.x; t < K; t += NTHREADS) u[t] += base[t];
+    __syncthreads();
+    off = 0;
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      const int n = b.n;
+      const int64_t nv = (int64_t)n * (n + 1) / 2;
+      T* Mt = b.W(W_T3);
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) {
+        const int p0 = (int)(k % n), q0 = (int)(k / n);
+        const int p = min(p0, q0), q = max(p0, q0);
+        const double v = u[off + svec_index(p, q)];
+        Mt[k] = (T)(p == q ? v : v / 1.4142135623730951);
+      }
+      __syncthreads();
+      // dX = sym(G M G'), dS = sym(Rd - A*(dy))
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_G), Mt, (T)0, b.W(W_T1), scr());
+      cta_gemm<T>(n, 0, 1, 0, 0, (T)1, b.W(W_T1), b.W(W_G), (T)0, b.W(W_T2), scr());
+      const T* dx = b.W(W_T2);
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) b.dX[k] = (double)dx[k];
+      __syncthreads();
+      cta_symmetrize<double>(n, b.dX);
+      jtprod_combine(b, P.dely, -1.0, b.Rd, nullptr, b.dS);
+      cta_symmetrize<double>(n, b.dS);
+      off += nv;
+    }
+    if (P.ns > 0) {
+      clin_tmv(P, P.dely, P.Rdlin, -1.0, P.delz);
+      for (int k = threadIdx.x; k < P.ns; k += NTHREADS) P.delx[k] = sqrt(P.x[k] / P.z[k]) * u[off + k];
+      __syncthreads();
+    }
   }
 
   // ================================================================ DualCentering

@@ -54,7 +54,8 @@ struct ProbDesc {
   int64_t Hf;    // FP32 Schur matrix m*m (mixed), -1 if absent
   int64_t Lf;    // FP32 Schur factor m*m (mixed), -1 if absent
   int64_t traj;  // FP64 trajectory (max_iter+2)*TRAJ_FIELDS
-  int32_t ntraj, pad;
+  int32_t ntraj, K;  // K: rows of the QRSchur matrix (sum n(n+1)/2 + ns)
+  int64_t qr;    // FP64 QRSchur workspace: B (K*m), tau (m), scale (m), base (K), dir (K); -1 if absent
 };
 
 // constraint structure of a block (detected at upload)

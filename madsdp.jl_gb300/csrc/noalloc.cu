@@ -139,6 +139,8 @@ extern "C" int msdp_solve_static(const msdp_problem_desc* prob, const msdp_compo
   pd.H64 = d64; d64 += (int64_t)m * m;
   pd.Hf = -1; pd.Lf = -1;
   pd.ntraj = 0;
+  pd.qr = -1;
+  pd.K = 0;
   pd.traj = d64;
   for (int i = 0; i < nb; ++i) {
     const int64_t n = prob->sides[i];

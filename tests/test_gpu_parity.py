@@ -97,14 +97,15 @@ X_FULL = np.array([[2.0, 0.3, 0.1], [0.3, 3.0, 0.4], [0.1, 0.4, 4.0]])
 S_FULL = np.array([[4.0, -0.2, 0.1], [-0.2, 2.0, 0.3], [0.1, 0.3, 3.0]])
 
 
+@pytest.mark.parametrize("schur", ["DenseCholesky", "QRSchur"])
 @pytest.mark.parametrize("scalars", [0, 2])
 @pytest.mark.parametrize("diagonal", [True, False])
-def test_newton_identities(gpu_ctx, scalars, diagonal):
+def test_newton_identities(gpu_ctx, scalars, diagonal, schur):
     """test/qr_schur.jl:16-66 through the component entry points."""
     model = g.qr_example(scalars)
     X0 = np.diag([2.0, 3.0, 4.0]) if diagonal else X_FULL
     S0 = np.diag([4.0, 2.0, 3.0]) if diagonal else S_FULL
-    bt = M.Batch([model], initial_point=M.ScaledIdentity())
+    bt = M.Batch([model], initial_point=M.ScaledIdentity(), schur=getattr(M, schur)())
     bt.initialize()
     bt.set_iterate(0, X=[X0], S=[S0])
     bt.update_residuals()
@@ -263,3 +264,43 @@ def test_dual_centering_trajectory(gpu_ctx):
     compare_trajectories(s.trajectory(), ref.trajectory)
     st = s.stats
     assert st["n_newton"] > 0 and st["n_predictor"] > 0
+
+
+# ------------------------------------------------------------------ QRSchur
+def test_qr_solves_psd_and_lp(gpu_ctx):
+    """test/qr_schur.jl:68-91."""
+    from madsdp_gpu.model import Model
+    lp = Model([], [], np.array([1.0]), np.array([1.0, 2.0]), np.array([[1.0, 1.0]]))
+    for model in (g.qr_example(0), g.qr_example(2), lp):
+        s = gpu_solve(model, schur=M.QRSchur(), initial_point=M.ScaledIdentity(), step=M.CholeskyBacktrack())
+        assert s.status == M.Status.SOLVE_SUCCEEDED
+        assert max(s.inf_pr, s.inf_du, s.inf_compl) <= 1e-7
+        ref = o.Solver(model, schur=o.QRSchur(), initial_point=o.ScaledIdentity(), step=o.CholeskyBacktrack()).solve()
+        scale = max(1.0, abs(ref.primal_objective()) + abs(ref.dual_objective()))
+        assert abs(s.primal_objective() - ref.primal_objective()) <= 1e-7 * scale
+        assert abs(s.iter - ref.iter) <= 1
+
+
+def test_qr_matches_dense_cholesky_on_sos(gpu_ctx):
+    model = g.sos_hankel(8, seed=21)
+    a = gpu_solve(model, schur=M.QRSchur())
+    b = gpu_solve(model)
+    assert a.status == b.status == M.Status.SOLVE_SUCCEEDED
+    assert abs(a.primal_objective() - b.primal_objective()) <= 1e-7 * max(1.0, abs(b.primal_objective()))
+
+
+def test_qr_unsupported_and_rank_deficient(gpu_ctx):
+    """test/qr_schur.jl:93-139."""
+    from madsdp_gpu.model import Model
+    with pytest.raises(ValueError):
+        M.MadSDPSolver(g.qr_example(), schur=M.QRSchur(), direction=M.HKM())
+    with pytest.raises(ValueError):
+        M.MadSDPSolver(g.qr_example(), schur=M.QRSchur(), algorithm=M.DualCentering())
+    with pytest.raises(ValueError):
+        M.MadSDPSolver(g.qr_example(), schur=M.QRSchur(), precision="mixed")
+    zero = Model([np.ones((1, 1))], [[np.zeros((1, 1))]], np.array([0.0]))
+    assert gpu_solve(zero, schur=M.QRSchur()).status == M.Status.ERROR_IN_STEP_COMPUTATION
+    for d, mats in ((1, [np.ones((1, 1)), np.ones((1, 1))]),
+                    (2, [np.diag([1.0, 0.0]), np.diag([1.0, 0.0])])):
+        model = Model([np.eye(d)], [mats], np.ones(2))
+        assert gpu_solve(model, schur=M.QRSchur()).status == M.Status.ERROR_IN_STEP_COMPUTATION
