@@ -184,8 +184,7 @@ int msdp_batch_create(msdp_context* ctx, const msdp_problem_desc* probs, int32_t
   }
   if (c.schur == MSDP_QR_SCHUR && c.precision != MSDP_FP64)
     return fail(ctx, MSDP_ERR_INVALID_ARGUMENT, "QRSchur requires Float64 data.");
-  if (c.schur == MSDP_MADNLP_SCHUR)
-    return fail(ctx, MSDP_ERR_UNSUPPORTED, "MadNLPSchur is not built into the device kernel");
+
   if (c.initial_point == MSDP_SCALED_IDENTITY && c.scale != 0.0 && !(std::isfinite(c.scale) && c.scale > 0.0))
     return fail(ctx, MSDP_ERR_INVALID_ARGUMENT, "The identity scale must be finite and positive.");
   if (o.max_iter < 0 || o.max_schur_reg < 0) return fail(ctx, MSDP_ERR_INVALID_ARGUMENT, "invalid options");
@@ -246,6 +245,8 @@ int msdp_batch_create(msdp_context* ctx, const msdp_problem_desc* probs, int32_t
     pd.K = (int32_t)K;
     if (c.schur == MSDP_QR_SCHUR) { pd.qr = o64; o64 = align4(o64 + K * m + 2 * m + 2 * K); }
     else pd.qr = -1;
+    if (c.schur == MSDP_MADNLP_SCHUR) { pd.piv = o64; o64 = align4(o64 + m); }
+    else pd.piv = -1;
     double nnz_sum = 0.0;
     for (int i = 0; i < d.nblocks; ++i, ++bi) {
       BlockDesc& bd = b->hblk[bi];

@@ -63,6 +63,7 @@ struct Prob {
   int ntraj;
   int K;
   double *qrB, *qrtau, *qrscale, *qrbase, *qrdir;
+  double* piv;
 };
 
 __device__ __forceinline__ Prob make_prob(const BatchDev& B, int p) {
@@ -101,6 +102,7 @@ __device__ __forceinline__ Prob make_prob(const BatchDev& B, int p) {
   } else {
     P.qrB = P.qrtau = P.qrscale = P.qrbase = P.qrdir = nullptr;
   }
+  P.piv = d.piv >= 0 ? B.d64 + d.piv : nullptr;
   return P;
 }
 
@@ -696,7 +698,9 @@ struct Algo {
         for (int64_t k = threadIdx.x; k < mm; k += NTHREADS) A[k] = H[k];
         __syncthreads();
       }
-      bool ok = cta_potrf<T>(m, A, m, &sh.flag);
+      bool ok = (prm.schur == MSDP_MADNLP_SCHUR)
+                    ? cta_sytrf_lower<T>(m, A, m, P.piv, (T*)P.wm, &sh.rb, &sh.flag)
+                    : cta_potrf<T>(m, A, m, &sh.flag);
       if (ok) {
         if (A != L) {
           for (int64_t k = threadIdx.x; k < mm; k += NTHREADS) L[k] = A[k];
@@ -1599,6 +1603,12 @@ __device__ void staged_potrs(int m, const T* L, double* x, unsigned char* smem) 
 }
 
 template <> __device__ void Algo<double>::schur_solve(double* x) {
+  if (prm.schur == MSDP_MADNLP_SCHUR) {
+    // MadNLPSchur: Bunch-Kaufman solve (src/kkt.jl:27-32)
+    if ((threadIdx.x >> 5) == 0) warp_sytrs_lower<double, double>(P.m, P.H64, P.m, P.piv, x);
+    __syncthreads();
+    return;
+  }
   staged_potrs<double>(P.m, P.H64, x, smem);
 }
 

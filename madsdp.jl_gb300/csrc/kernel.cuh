@@ -176,6 +176,7 @@ __device__ void iterate_one(const BatchDev& B, Prob& P, unsigned char* smem, Sha
   if constexpr (MIXED != 0) {
     int phase = (int)P.sc[SC_PHASE];
     if (phase == 0 && fmax(fmax(P.sc[SC_INFPR], P.sc[SC_INFDU]), P.sc[SC_GAP]) < prm.switch_tol) phase = 1;
+    if (prm.schur != MSDP_DENSE_CHOLESKY) phase = 1;  // the FP32 phase factors by Cholesky only
     if (phase == 0) {
       const double pr_old = P.sc[SC_INFPR];
       Algo<float> A(B, P, smem, sh);

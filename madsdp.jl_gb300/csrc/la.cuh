@@ -716,3 +716,181 @@ __device__ void warp_lanczos_full(int n, const T* Z, T* Q, T* a, T* bb, T* w, T*
     }
   }
 }
+
+// ---------------------------------------------------------------- Bunch-Kaufman
+// Symmetric indefinite factorization A = P L D L' P' with 1x1 and 2x2
+// pivots (Bunch-Kaufman partial pivoting, the LAPACK sytf2 "lower"
+// algorithm), in place on the lower triangle of the m x m matrix `a`
+// (leading dimension lda).  piv[k] = kp for a 1x1 pivot (rows k and kp
+// swapped); piv[k] = piv[k+1] = -(kp + 1) for a 2x2 pivot whose second row
+// was swapped with kp.  Returns false when a pivot column is exactly zero
+// (singular).  `work` holds 2m scratch values.
+template <class T>
+__device__ bool cta_sytrf_lower(int m, T* a, int lda, double* piv, T* work, RedBuf* rb, int* flag) {
+  const T alpha = (T)((1.0 + sqrt(17.0)) / 8.0);
+  auto A = [&](int i, int j) -> T& { return a[i + (int64_t)j * lda]; };
+  int k = 0;
+  while (k < m) {
+    // colmax and its row (smallest index on ties)
+    double cm = -1.0;
+    int ci = m;
+    for (int i = k + 1 + threadIdx.x; i < m; i += NTHREADS) {
+      const double v = fabs((double)A(i, k));
+      if (v > cm) { cm = v; ci = i; }
+    }
+    // block argmax: encode (value, -index) through two reductions
+    const double colmax_all = block_max(cm, rb);
+    int cand = (cm == colmax_all && cm >= 0.0) ? ci : m;
+    // smallest index attaining the max
+    if (threadIdx.x == 0) *flag = m;
+    __syncthreads();
+    if (cand < m) atomicMin(flag, cand);
+    __syncthreads();
+    const int imax = *flag;
+    __syncthreads();
+    const double colmax = (k + 1 < m) ? fmax(colmax_all, 0.0) : 0.0;
+    const double absakk = fabs((double)A(k, k));
+    if (!(fmax(absakk, colmax) > 0.0)) return false;  // zero column (or NaN): singular
+    int kp = k, kstep = 1;
+    if (!(absakk >= (double)alpha * colmax)) {
+      // rowmax: largest off-diagonal magnitude in row/column imax of the trailing matrix
+      double rm = 0.0;
+      for (int j = k + threadIdx.x; j < m; j += NTHREADS) {
+        if (j == imax) continue;
+        const double v = j < imax ? fabs((double)A(imax, j)) : fabs((double)A(j, imax));
+        rm = fmax(rm, v);
+      }
+      const double rowmax = block_max(rm, rb);
+      if (absakk >= (double)alpha * colmax * (colmax / rowmax)) kp = k;
+      else if (fabs((double)A(imax, imax)) >= (double)alpha * rowmax) kp = imax;
+      else { kp = imax; kstep = 2; }
+    }
+    const int kk = k + kstep - 1;
+    if (kp != kk) {
+      // symmetric interchange of rows/columns kk and kp in the trailing matrix
+      for (int i = kp + 1 + threadIdx.x; i < m; i += NTHREADS) {
+        const T t = A(i, kk); A(i, kk) = A(i, kp); A(i, kp) = t;
+      }
+      for (int j = kk + 1 + threadIdx.x; j < kp; j += NTHREADS) {
+        const T t = A(j, kk); A(j, kk) = A(kp, j); A(kp, j) = t;
+      }
+      if (threadIdx.x == 0) {
+        const T t = A(kk, kk); A(kk, kk) = A(kp, kp); A(kp, kp) = t;
+        if (kstep == 2) { const T u = A(k + 1, k); A(k + 1, k) = A(kp, k); A(kp, k) = u; }
+      }
+      __syncthreads();
+    }
+    if (kstep == 1) {
+      const T r1 = (T)1 / A(k, k);
+      const int r = m - k - 1;
+      const int rr = r * r;
+      for (int idx = threadIdx.x; idx < rr; idx += NTHREADS) {
+        const int ii = idx % r, jj = idx / r;
+        if (ii >= jj) {
+          const int i = k + 1 + ii, j = k + 1 + jj;
+          A(i, j) -= r1 * A(i, k) * A(j, k);
+        }
+      }
+      __syncthreads();
+      for (int i = k + 1 + threadIdx.x; i < m; i += NTHREADS) A(i, k) *= r1;
+      if (threadIdx.x == 0) piv[k] = (double)kp;
+      __syncthreads();
+    } else {
+      if (k + 2 < m) {
+        T d21 = A(k + 1, k);
+        const T d11 = A(k + 1, k + 1) / d21, d22 = A(k, k) / d21;
+        const T t = (T)1 / (d11 * d22 - (T)1);
+        d21 = t / d21;
+        T* wk = work;
+        T* wk1 = work + m;
+        for (int j = k + 2 + threadIdx.x; j < m; j += NTHREADS) {
+          wk[j] = d21 * (d11 * A(j, k) - A(j, k + 1));
+          wk1[j] = d21 * (d22 * A(j, k + 1) - A(j, k));
+        }
+        __syncthreads();
+        const int r = m - k - 2;
+        const int rr = r * r;
+        for (int idx = threadIdx.x; idx < rr; idx += NTHREADS) {
+          const int ii = idx % r, jj = idx / r;
+          if (ii >= jj) {
+            const int i = k + 2 + ii, j = k + 2 + jj;
+            A(i, j) -= A(i, k) * wk[j] + A(i, k + 1) * wk1[j];
+          }
+        }
+        __syncthreads();
+        for (int j = k + 2 + threadIdx.x; j < m; j += NTHREADS) { A(j, k) = wk[j]; A(j, k + 1) = wk1[j]; }
+      }
+      if (threadIdx.x == 0) { piv[k] = (double)(-(kp + 1)); piv[k + 1] = (double)(-(kp + 1)); }
+      __syncthreads();
+    }
+    k += kstep;
+  }
+  return true;
+}
+
+// Solve with the factorization of cta_sytrf_lower (the LAPACK sytrs
+// "lower" algorithm), one warp, x in place.
+template <class T, class V>
+__device__ void warp_sytrs_lower(int m, const T* a, int lda, const double* piv, V* x) {
+  const int lane = threadIdx.x & 31;
+  auto A = [&](int i, int j) -> V { return (V)a[i + (int64_t)j * lda]; };
+  int k = 0;
+  while (k < m) {
+    if (piv[k] >= 0.0) {
+      const int kp = (int)piv[k];
+      if (lane == 0 && kp != k) { const V t = x[k]; x[k] = x[kp]; x[kp] = t; }
+      __syncwarp();
+      const V xk = x[k];
+      for (int i = k + 1 + lane; i < m; i += 32) x[i] -= A(i, k) * xk;
+      __syncwarp();
+      if (lane == 0) x[k] = xk / A(k, k);
+      __syncwarp();
+      k += 1;
+    } else {
+      const int kp = (int)(-piv[k]) - 1;
+      if (lane == 0 && kp != k + 1) { const V t = x[k + 1]; x[k + 1] = x[kp]; x[kp] = t; }
+      __syncwarp();
+      const V xk = x[k], xk1 = x[k + 1];
+      for (int i = k + 2 + lane; i < m; i += 32) x[i] -= A(i, k) * xk + A(i, k + 1) * xk1;
+      __syncwarp();
+      if (lane == 0) {
+        const V akm1k = A(k + 1, k);
+        const V akm1 = A(k, k) / akm1k, ak = A(k + 1, k + 1) / akm1k;
+        const V denom = akm1 * ak - (V)1;
+        const V bkm1 = xk / akm1k, bk = xk1 / akm1k;
+        x[k] = (ak * bkm1 - bk) / denom;
+        x[k + 1] = (akm1 * bk - bkm1) / denom;
+      }
+      __syncwarp();
+      k += 2;
+    }
+  }
+  k = m - 1;
+  while (k >= 0) {
+    if (piv[k] >= 0.0) {
+      V s = 0;
+      for (int i = k + 1 + lane; i < m; i += 32) s += A(i, k) * x[i];
+      s = warp_sum(s);
+      if (lane == 0) {
+        x[k] -= s;
+        const int kp = (int)piv[k];
+        if (kp != k) { const V t = x[k]; x[k] = x[kp]; x[kp] = t; }
+      }
+      __syncwarp();
+      k -= 1;
+    } else {
+      V s = 0, s1 = 0;
+      for (int i = k + 1 + lane; i < m; i += 32) { s += A(i, k) * x[i]; s1 += A(i, k - 1) * x[i]; }
+      s = warp_sum(s);
+      s1 = warp_sum(s1);
+      if (lane == 0) {
+        x[k] -= s;
+        x[k - 1] -= s1;
+        const int kp = (int)(-piv[k]) - 1;
+        if (kp != k) { const V t = x[k]; x[k] = x[kp]; x[kp] = t; }
+      }
+      __syncwarp();
+      k -= 2;
+    }
+  }
+}

@@ -56,6 +56,7 @@ struct ProbDesc {
   int64_t traj;  // FP64 trajectory (max_iter+2)*TRAJ_FIELDS
   int32_t ntraj, K;  // K: rows of the QRSchur matrix (sum n(n+1)/2 + ns)
   int64_t qr;    // FP64 QRSchur workspace: B (K*m), tau (m), scale (m), base (K), dir (K); -1 if absent
+  int64_t piv;   // FP64 MadNLPSchur pivot record (m), -1 if absent
 };
 
 // constraint structure of a block (detected at upload)

@@ -140,6 +140,7 @@ extern "C" int msdp_solve_static(const msdp_problem_desc* prob, const msdp_compo
   pd.Hf = -1; pd.Lf = -1;
   pd.ntraj = 0;
   pd.qr = -1;
+  pd.piv = -1;
   pd.K = 0;
   pd.traj = d64;
   for (int i = 0; i < nb; ++i) {

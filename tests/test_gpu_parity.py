@@ -54,12 +54,13 @@ def test_component_matrix(gpu_ctx, direction, step, centering):
         assert abs(s.primal_objective() - expected) <= cm["atol"]
 
 
-def test_mc_psd_start(gpu_ctx):
+@pytest.mark.parametrize("schur", ["DenseCholesky", "MadNLPSchur"])
+def test_mc_psd_start(gpu_ctx, schur):
     case = KA["mc_psd_start"]
     L = laplacian(g.weighted_4node_W())
     ip = M.InitialPoint([np.eye(4)], -(1 + np.abs(L / 4).sum(axis=0)))
     s = gpu_solve(build("maxcut_weighted4"), direction=M.HKM(), step=M.CholeskyBacktrack(),
-                  centering=M.AdaptiveMu(), initial_point=ip)
+                  centering=M.AdaptiveMu(), initial_point=ip, schur=getattr(M, schur)())
     assert s.status == M.Status.SOLVE_SUCCEEDED
     assert abs(s.primal_objective() - case["objective"]) <= case["atol"]
     assert s.inf_du < case["inf_du_below"]
@@ -234,11 +235,11 @@ def test_dual_centering_known_answers(gpu_ctx, case):
 
 
 def test_dual_centering_theoretical_A(gpu_ctx):
-    # test/dual_runtests.jl:76-101 (second half; DenseCholesky on the device)
+    # test/dual_runtests.jl:76-101 (second half, with the MadNLPSchur solver)
     L = laplacian(g.weighted_4node_W())
     y0 = -(1 + np.abs(L / 4).sum(axis=0))
     s = gpu_solve(build("maxcut_weighted4"), algorithm=M.DualCentering(A=None),
-                  initial_point=M.InitialPoint([np.eye(4)], y0), tol=1e-6, max_iter=300)
+                  initial_point=M.InitialPoint([np.eye(4)], y0), schur=M.MadNLPSchur(), tol=1e-6, max_iter=300)
     assert s.status == M.Status.SOLVE_SUCCEEDED
     assert abs(s.dual_objective() + 18.0) <= 1e-3
 
@@ -304,3 +305,26 @@ def test_qr_unsupported_and_rank_deficient(gpu_ctx):
                     (2, [np.diag([1.0, 0.0]), np.diag([1.0, 0.0])])):
         model = Model([np.eye(d)], [mats], np.ones(2))
         assert gpu_solve(model, schur=M.QRSchur()).status == M.Status.ERROR_IN_STEP_COMPUTATION
+
+
+# ------------------------------------------------------------------ MadNLPSchur (Bunch-Kaufman)
+@pytest.mark.parametrize("model_name", ["maxcut_weighted4", "mixed_lp", "qr_example2"])
+def test_madnlp_schur_matches_oracle(gpu_ctx, model_name):
+    model = build(model_name)
+    s = gpu_solve(model, schur=M.MadNLPSchur())
+    ref = o.Solver(build(model_name), schur=o.MadNLPSchur()).solve()
+    assert s.status == ref.status == M.Status.SOLVE_SUCCEEDED
+    scale = max(1.0, abs(ref.primal_objective()) + abs(ref.dual_objective()))
+    assert abs(s.primal_objective() - ref.primal_objective()) <= 1e-7 * scale
+    assert abs(s.iter - ref.iter) <= 1
+
+
+def test_madnlp_schur_batch_sos(gpu_ctx):
+    models = sos_batch(n=6, seed=3)
+    a = M.Batch(models, schur=M.MadNLPSchur())
+    a.solve()
+    b = M.Batch(models)
+    b.solve()
+    for sa, sb in zip(a.all_stats(), b.all_stats()):
+        assert sa["status"] == sb["status"] == M.Status.SOLVE_SUCCEEDED
+        assert abs(sa["pobj"] - sb["pobj"]) <= 1e-7 * max(1.0, abs(sb["pobj"]) + abs(sb["dobj"]))
