@@ -103,8 +103,8 @@ typedef struct msdp_options {
   double mu_min;           /* 1e-14 */
   double regularize_schur; /* 1e-12 */
   int32_t datasparsity;    /* 8 (accepted, constraint storage is chosen per problem) */
-  int32_t pad0;
-  double switch_tol;       /* MSDP_MIXED: FP32 iterations while max(inf_pr, inf_du, gap) > switch_tol */
+  int32_t mixed_refine;    /* MSDP_MIXED: refinement passes of each FP32 direction against the float64 primal defect (2) */
+  double switch_tol;       /* MSDP_MIXED: FP32 iterations while max(inf_pr, inf_du, gap) > switch_tol (0) */
 } msdp_options;
 
 /* One problem in the form of LowRankOpt.Model(C, A, b, d_lin, C_lin, sides). */

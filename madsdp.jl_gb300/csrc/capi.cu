@@ -110,7 +110,8 @@ void msdp_default_options(msdp_options* o) {
   o->mu_min = 1e-14;
   o->regularize_schur = 1e-12;
   o->datasparsity = 8;
-  o->switch_tol = 1e-3;
+  o->mixed_refine = 2;
+  o->switch_tol = 0.0;
 }
 
 int msdp_device_count(void) {
@@ -208,6 +209,7 @@ int msdp_batch_create(msdp_context* ctx, const msdp_problem_desc* probs, int32_t
   prm.tol = o.tol; prm.max_wall_time = o.max_wall_time; prm.mu_min = o.mu_min;
   prm.regularize_schur = o.regularize_schur; prm.switch_tol = o.switch_tol;
   prm.max_iter = o.max_iter; prm.max_schur_reg = o.max_schur_reg;
+  prm.mixed_refine = std::max(0, std::min(o.mixed_refine, 8));
 
   // ---- layout pass
   int64_t nblk_total = 0;

@@ -1051,8 +1051,112 @@ struct Algo {
     schur_solve(P.dely);
     PROF_END(s, SC_T_SOLVE);
     PROF_BEGIN(d);
-    directions(mu, corrected);
+    if (sizeof(T) == 4 && prm.mixed_refine > 0) {
+      // FP32 phase: directions with E applied in float64 to the FP32
+      // scaling, then `mixed_refine` passes of Schur solves on the float64
+      // primal defect r = Rp - A(dX) - C_lin dx, so that the primal
+      // equation holds to float64 accuracy for that scaling.
+      directions64(mu, corrected, !corrected);
+      for (int pass = 0; pass < prm.mixed_refine; ++pass) {
+        for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.h[j] = P.Rp[j];
+        __syncthreads();
+        for (int i = 0; i < P.nblocks; ++i) {
+          Blk<T> b = blk(i);
+          for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) b.buf[k] = -b.dX[k];
+          __syncthreads();
+          jprod_add(b, P.m, b.buf, P.h);
+        }
+        if (P.ns > 0) clin_mv(P, P.delx, -1.0, P.h);
+        schur_solve(P.h);
+        for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.dely[j] += P.h[j];
+        __syncthreads();
+        directions64(mu, corrected, false);
+      }
+      // remaining float64 primal defect, relative as inf_pr (the caller
+      // rejects an FP32 direction that does not satisfy the primal equation)
+      for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.h[j] = P.Rp[j];
+      __syncthreads();
+      for (int i = 0; i < P.nblocks; ++i) {
+        Blk<T> b = blk(i);
+        for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) b.buf[k] = -b.dX[k];
+        __syncthreads();
+        jprod_add(b, P.m, b.buf, P.h);
+      }
+      if (P.ns > 0) clin_mv(P, P.delx, -1.0, P.h);
+      double dmax = 0.0, rmax = 0.0;
+      for (int j = threadIdx.x; j < P.m; j += NTHREADS) {
+        dmax = fmax(dmax, fabs(P.h[j]));
+        rmax = fmax(rmax, fabs(P.Rp[j]));
+      }
+      dmax = block_max(dmax, &sh.rb);
+      rmax = block_max(rmax, &sh.rb);
+      if (threadIdx.x == 0) {
+        const double bn = fmax(1.0, P.sc[SC_BNORM]);
+        sh.bc[7] = (dmax / bn > fmax(0.1 * rmax / bn, 0.01 * prm.tol)) ? 1.0 : 0.0;
+      }
+      __syncthreads();
+    } else {
+      directions(mu, corrected);
+      if (threadIdx.x == 0) sh.bc[7] = 0.0;
+      __syncthreads();
+    }
     PROF_END(d, SC_T_DIRECTIONS);
+  }
+  // whether the last solve_directions left a primal defect above its bound
+  __device__ __forceinline__ bool inexact_direction() const { return sh.bc[7] != 0.0; }
+
+  // directions! with E(M) evaluated in float64 on the compute-type scaling
+  // (NT: W M W; HKM: sym(X M S^-1)); E(Rd) is formed when `fresh_erd`.
+  __noinline__ __device__ void directions64(double mu, bool corrected, bool fresh_erd) {
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      Blk<double> bd = make_blk<double>(B, P, i);
+      const int n = b.n;
+      const bool rdnz = b.bsc[BS_RDNZ] != 0.0;
+      double* L64 = bd.W(W_W);
+      double* R64 = bd.W(W_SI);
+      double* erd = bd.W(W_ERD);
+      double* e1 = bd.W(W_T1);
+      double* tmp = bd.W(W_T3);
+      if (fresh_erd) {
+        const T* Lc = is_nt() ? b.W(W_W) : xt(b);
+        const T* Rc = is_nt() ? b.W(W_W) : b.W(W_SI);
+        for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) { L64[k] = (double)Lc[k]; R64[k] = (double)Rc[k]; }
+        __syncthreads();
+        if (rdnz) {
+          cta_gemm<double>(n, 0, 0, 0, 0, 1.0, L64, b.Rd, 0.0, tmp, scr());
+          cta_gemm<double>(n, 0, 0, 0, 0, 1.0, tmp, R64, 0.0, erd, scr());
+          cta_symmetrize<double>(n, erd);
+        }
+      }
+      jtprod_combine(b, P.dely, 1.0, nullptr, nullptr, b.ATy);
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) b.dS[k] = b.Rd[k] - b.ATy[k];
+      __syncthreads();
+      cta_symmetrize<double>(n, b.dS);
+      cta_gemm<double>(n, 0, 0, 0, 0, 1.0, L64, b.ATy, 0.0, tmp, scr());
+      cta_gemm<double>(n, 0, 0, 0, 0, 1.0, tmp, R64, 0.0, e1, scr());
+      cta_symmetrize<double>(n, e1);
+      const T* Si = b.W(W_SI);
+      const T* corr = b.W(W_CORR);
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) {
+        double v = mu * (double)Si[k] - b.X[k] + e1[k];
+        if (rdnz) v -= erd[k];
+        if (corrected) v += (double)corr[k];
+        b.dX[k] = v;
+      }
+      __syncthreads();
+      cta_symmetrize<double>(n, b.dX);
+    }
+    if (P.ns > 0) {
+      clin_tmv(P, P.dely, P.Rdlin, -1.0, P.delz);
+      for (int k = threadIdx.x; k < P.ns; k += NTHREADS) {
+        const double x = P.x[k], zi = P.zinv[k];
+        double v = mu * zi - x - x * zi * P.delz[k];
+        if (corrected) v += P.corrlin[k];
+        P.delx[k] = v;
+      }
+      __syncthreads();
+    }
   }
 
   // One Mehrotra predictor-corrector iteration (src/primal_dual.jl:85-101).
@@ -1063,6 +1167,7 @@ struct Algo {
     if (threadIdx.x == 0) P.sc[SC_MU] = mu;
     __syncthreads();
     solve_directions(0.0, false);
+    if (!strict && inexact_direction()) return false;
     double a_aff, b_aff;
     {
       PROF_BEGIN(st);
@@ -1079,6 +1184,7 @@ struct Algo {
       PROF_END(c, SC_T_CORRECTION);
     }
     solve_directions(sigma * mu, true);
+    if (!strict && inexact_direction()) return false;
     double a, bt;
     {
       PROF_BEGIN(st);
@@ -1097,6 +1203,7 @@ struct Algo {
     if (!prepare() || !factorize_schur()) return false;
     const double mu0 = P.sc[SC_MU];
     solve_directions(mu0, false);
+    if (!strict && inexact_direction()) return false;
     double a, bt;
     step_lengths(a, bt);
     if (!strict && !(fmin(a, bt) >= 0.2)) return false;
@@ -1591,12 +1698,13 @@ __device__ void staged_potrs(int m, const T* L, double* x, unsigned char* smem) 
   const int64_t mm = (int64_t)m * m;
   double* sx = (double*)smem;
   T* sL = (T*)(smem + (((int64_t)m * sizeof(double) + 15) & ~(int64_t)15));
-  const bool stageL = ((int64_t)m * sizeof(double) + 16 + mm * (int64_t)sizeof(T)) <= MSDP_SMEM_BYTES;
+  double* rd = (double*)(smem + MSDP_SMEM_BYTES) - m;  // reciprocal diagonal at the end of the scratch
+  const bool stageL = ((int64_t)m * sizeof(double) * 2 + 16 + mm * (int64_t)sizeof(T)) <= MSDP_SMEM_BYTES;
   for (int j = threadIdx.x; j < m; j += NTHREADS) sx[j] = x[j];
   if (stageL)
     for (int64_t k = threadIdx.x; k < mm; k += NTHREADS) sL[k] = L[k];
   __syncthreads();
-  if ((threadIdx.x >> 5) == 0) warp_potrs<T, double>(m, stageL ? sL : L, sx);
+  if ((threadIdx.x >> 5) == 0) warp_potrs<T, double>(m, stageL ? sL : L, sx, rd);
   __syncthreads();
   for (int j = threadIdx.x; j < m; j += NTHREADS) x[j] = sx[j];
   __syncthreads();

@@ -193,7 +193,9 @@ __device__ void iterate_one(const BatchDev& B, Prob& P, unsigned char* smem, Sha
         const double err = fmax(0.0, rp - (1.0 - a) * pr_old) / fmax(a, 1e-300);
         if (threadIdx.x == 0) {
           P.sc[SC_N32] += 1.0;
-          if (err > 0.1 * pr_old) P.sc[SC_PHASE] = 1.0;
+          // a primal residual already below a tenth of the tolerance needs no
+          // more accuracy than FP32 gives
+          if (err > fmax(0.1 * pr_old, 0.1 * prm.tol)) P.sc[SC_PHASE] = 1.0;
         }
         __syncthreads();
         return;

@@ -359,8 +359,12 @@ __device__ bool cta_jacobi_svd_g(int n, T* M, T* B, T* sigma, int max_sweeps, in
         const T scale_pq = Num<T>::sqrt_(app) * Num<T>::sqrt_(aqq);
         if (p >= 0 && fabs(apq) > tol * scale_pq) {
           if (fabs(apq) > big_tol * scale_pq) big = 1;
-          const T zeta = (aqq - app) / ((T)2 * apq);
-          const T t = (zeta >= (T)0 ? (T)1 : (T)-1) / (fabs(zeta) + Num<T>::sqrt_((T)1 + zeta * zeta));
+          // the angle only needs float accuracy (the next sweep removes what
+          // is left); c and s are formed in T so the rotation is orthogonal
+          // to T's rounding
+          const float zf = (float)((aqq - app) / ((T)2 * apq));
+          const float tf = (zf >= 0.0f ? 1.0f : -1.0f) / (fabsf(zf) + sqrtf(1.0f + zf * zf));
+          const T t = (T)tf;
           const T c = Num<T>::rsqrt_((T)1 + t * t), sn = c * t;
           T* mp = M + (int64_t)p * n;
           T* mq = M + (int64_t)q * n;
@@ -430,7 +434,68 @@ __device__ __forceinline__ int sturm_count(int k, const T* a, const T* b, T x, T
 // Smallest eigenvalue of the tridiagonal (a, b) by warp-parallel multisection.
 // Called by one full warp; every lane returns the result.
 template <class T>
-__device__ T warp_tridiag_eigmin(int k, const T* a, const T* b) {
+__device__ T warp_tridiag_eigmin_t(int k, const T* a, const T* b);
+
+template <class T>
+__device__ __forceinline__ T warp_tridiag_eigmin(int k, const T* a, const T* b) {
+  return warp_tridiag_eigmin_t<T>(k, a, b);
+}
+
+// float64: bracket the eigenvalue with float Sturm counts (cheap divisions),
+// then a few float64 multisection rounds inside the bracket.
+template <>
+__device__ __forceinline__ double warp_tridiag_eigmin<double>(int k, const double* a, const double* b) {
+  const int lane = threadIdx.x & 31;
+  double scale = 0;
+  for (int i = 0; i < k; ++i) scale = fmax(scale, fabs(a[i]) + (i > 0 ? fabs(b[i]) : 0.0) + (i + 1 < k ? fabs(b[i + 1]) : 0.0));
+  if (!(scale > 0.0) || !isfinite(scale)) return warp_tridiag_eigmin_t<double>(k, a, b);
+  // float multisection on the scaled tridiagonal (entries in [-1, 1])
+  const float inv = (float)(1.0 / scale);
+  float lo = -1.0f, hi = 1.0f;
+  const float pivf = 1e-30f;
+  for (int it = 0; it < 5; ++it) {
+    const float x = lo + (hi - lo) * (float)(lane + 1) / 33.0f;
+    int c = 0;
+    float d = (float)a[0] * inv - x;
+    if (fabsf(d) < pivf) d = -pivf;
+    c += d < 0.0f;
+    for (int i = 1; i < k; ++i) {
+      const float bi = (float)b[i] * inv;
+      d = ((float)a[i] * inv - x) - bi * bi / d;
+      if (fabsf(d) < pivf) d = -pivf;
+      c += d < 0.0f;
+    }
+    const unsigned ball = __ballot_sync(0xffffffffu, c >= 1);
+    if (ball == 0) { lo = lo + (hi - lo) * 32.0f / 33.0f; continue; }
+    const int first = __ffs(ball) - 1;
+    const float nhi = lo + (hi - lo) * (float)(first + 1) / 33.0f;
+    const float nlo = first == 0 ? lo : lo + (hi - lo) * (float)first / 33.0f;
+    lo = nlo; hi = nhi;
+  }
+  // widen by the float rounding of the scaled problem and polish in float64
+  const double w = 4e-6 * fmax(1.0, fabs((double)lo) + fabs((double)hi));
+  double dlo = ((double)lo - w) * scale, dhi = ((double)hi + w) * scale;
+  const double pivmin = 4.93e-32 * fmax(scale, 1e-30);
+  // confirm the bracket (fall back to the full search if rounding moved it)
+  const int cl = sturm_count<double>(k, a, b, dlo, pivmin);
+  const int ch = sturm_count<double>(k, a, b, dhi, pivmin);
+  if (cl != 0 || ch < 1) return warp_tridiag_eigmin_t<double>(k, a, b);
+  for (int it = 0; it < 16; ++it) {
+    if (dhi - dlo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(dlo), fabs(dhi)) + pivmin) break;
+    const double x = dlo + (dhi - dlo) * (double)(lane + 1) / 33.0;
+    const int c = sturm_count<double>(k, a, b, x, pivmin);
+    const unsigned ball = __ballot_sync(0xffffffffu, c >= 1);
+    if (ball == 0) { dlo = dlo + (dhi - dlo) * 32.0 / 33.0; continue; }
+    const int first = __ffs(ball) - 1;
+    const double nhi = dlo + (dhi - dlo) * (double)(first + 1) / 33.0;
+    const double nlo = first == 0 ? dlo : dlo + (dhi - dlo) * (double)first / 33.0;
+    dlo = nlo; dhi = nhi;
+  }
+  return (dlo + dhi) / 2;
+}
+
+template <class T>
+__device__ T warp_tridiag_eigmin_t(int k, const T* a, const T* b) {
   const int lane = threadIdx.x & 31;
   T lo = 0, hi = 0, scale = 0;
   // Gershgorin interval
@@ -603,10 +668,13 @@ __device__ T warp_lanczos_eigmin(int n, const T* Z, T* Qs, int kq, T* Qg, T* a, 
 // Solve L L' x = b in place (L lower, ld m) by ONE warp; x (and L, when
 // the caller staged it) in shared memory.
 template <class T, class V>
-__device__ void warp_potrs(int m, const T* __restrict__ L, V* x) {
+__device__ void warp_potrs(int m, const T* __restrict__ L, V* x, V* rdiag) {
   const int lane = threadIdx.x & 31;
+  // reciprocal diagonal once (lanes in parallel) instead of a division per row
+  for (int k = lane; k < m; k += 32) rdiag[k] = (V)1 / (V)L[k + (int64_t)k * m];
+  __syncwarp();
   for (int k = 0; k < m; ++k) {
-    const V xk = x[k] / (V)L[k + (int64_t)k * m];
+    const V xk = x[k] * rdiag[k];
     __syncwarp();
     if (lane == 0) x[k] = xk;
     const T* lk = L + (int64_t)k * m;
@@ -618,7 +686,7 @@ __device__ void warp_potrs(int m, const T* __restrict__ L, V* x) {
     V s = 0;
     for (int i = k + 1 + lane; i < m; i += 32) s += (V)lk[i] * x[i];
     s = warp_sum(s);
-    if (lane == 0) x[k] = (x[k] - s) / (V)L[k + (int64_t)k * m];
+    if (lane == 0) x[k] = (x[k] - s) * rdiag[k];
     __syncwarp();
   }
 }

@@ -83,6 +83,7 @@ struct Params {
   // options
   double tol, max_wall_time, mu_min, regularize_schur, switch_tol;
   int32_t max_iter, max_schur_reg;
+  int32_t mixed_refine, pad1;
   // per-launch arguments
   int32_t op, max_iterations;
   double op_mu;

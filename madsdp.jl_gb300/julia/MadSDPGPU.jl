@@ -26,7 +26,7 @@ end
 
 struct Options
     tol::Float64; max_iter::Int32; max_schur_reg::Int32; max_wall_time::Float64
-    mu_min::Float64; regularize_schur::Float64; datasparsity::Int32; pad0::Int32
+    mu_min::Float64; regularize_schur::Float64; datasparsity::Int32; mixed_refine::Int32
     switch_tol::Float64
 end
 
@@ -118,7 +118,7 @@ function solve(model::LRO.Model; direction = MadSDP.NT(), step = MadSDP.EigenSte
         kw = Dict(options)
         o = Options(get(kw, :tol, o.tol), get(kw, :max_iter, o.max_iter), get(kw, :max_schur_reg, o.max_schur_reg),
                     get(kw, :max_wall_time, o.max_wall_time), get(kw, :mu_min, o.mu_min),
-                    get(kw, :regularize_schur, o.regularize_schur), o.datasparsity, 0, o.switch_tol)
+                    get(kw, :regularize_schur, o.regularize_schur), o.datasparsity, o.mixed_refine, o.switch_tol)
         comp = components(; algorithm, direction, step, centering, initial_point, schur, precision)
         ctx = Ref{Ptr{Cvoid}}(C_NULL)
         check(C_NULL, ccall((:msdp_context_create, LIB), Cint, (Cint, Ptr{Ptr{Cvoid}}), device, ctx), "context")

@@ -30,7 +30,7 @@ class Components(C.Structure):
 class Options(C.Structure):
     _fields_ = [
         ("tol", f64), ("max_iter", i32), ("max_schur_reg", i32), ("max_wall_time", f64),
-        ("mu_min", f64), ("regularize_schur", f64), ("datasparsity", i32), ("pad0", i32),
+        ("mu_min", f64), ("regularize_schur", f64), ("datasparsity", i32), ("mixed_refine", i32),
         ("switch_tol", f64),
     ]
 

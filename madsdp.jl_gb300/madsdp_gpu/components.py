@@ -166,7 +166,10 @@ class Options:
     max_schur_reg: int = 8
     datasparsity: int = 8
     # MSDP_MIXED: FP32 iterations while max(inf_pr, inf_du, gap) > switch_tol
-    switch_tol: float = 1e-3
+    switch_tol: float = 0.0
+    # MSDP_MIXED: refinement passes of each FP32 direction against the
+    # float64 primal defect
+    mixed_refine: int = 2
 
 
 PRECISIONS = {"fp64": 0, "mixed": 1}

@@ -129,7 +129,7 @@ def _options(opt: Options) -> _lib.Options:
     _lib.load().msdp_default_options(C.byref(o))
     o.tol, o.max_iter, o.max_wall_time = opt.tol, opt.max_iter, opt.max_wall_time
     o.mu_min, o.regularize_schur, o.max_schur_reg = opt.mu_min, opt.regularize_schur, opt.max_schur_reg
-    o.datasparsity, o.switch_tol = opt.datasparsity, opt.switch_tol
+    o.datasparsity, o.switch_tol, o.mixed_refine = opt.datasparsity, opt.switch_tol, opt.mixed_refine
     return o
 
 
