@@ -33,6 +33,10 @@ for _p in (ROOT, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
+# request mix of the served stream (Poisson arrivals); sizes are those one
+# CTA per request solves at interactive latency
+SERVE_MIX = {"sos_d": (5, 127), "maxcut_n": (20, 100), "dense_n": (8, 32), "dense_m": 200}
+
 METRIC = "SDP solves/sec + p50/p99 latency at 1e-7 gap: mixed/batched vs FP64 GPU vs CPU"
 UNIT = "solves/s"
 
@@ -93,6 +97,170 @@ def cpu_oracle_sample(ds, seed, seconds, cores):
     if env_keep is None:
         os.environ.pop("OMP_NUM_THREADS", None)
     return len(results) / elapsed, results, len(results)
+
+
+# ----------------------------------------------------------------- single large instances
+INSTANCE_WORKLOADS = {
+    # MaxCut, ER n = 100, p = 0.1, unit weights (the reference's benchmark/maxcut.jl shape)
+    "maxcut_n100": dict(kind="maxcut", n=100, p=0.1, weights="unit"),
+    # MaxCut at scale, ER n = 2000, p = 0.005, weights +-1
+    "maxcut_n2000": dict(kind="maxcut", n=2000, p=0.005, weights="pm1"),
+    # dense constraints, PSD blocks [200, 100, 50, 50] + 500 scalars, m = 2000
+    "dense_mixed_cones": dict(kind="dense", sides=[200, 100, 50, 50], ns=500, m=2000),
+}
+
+
+def instance_model(spec, seed):
+    from madsdp_gpu import generators as g
+    if spec["kind"] == "maxcut":
+        return g.maxcut(spec["n"], spec["p"], weights=spec["weights"], seed=seed)
+    return g.dense_random(spec["sides"], spec["ns"], spec["m"], seed=seed)
+
+
+def instance_flops_per_iteration(model) -> float:
+    """28 n^3 per block (NT scaling, E(.), correction, step lengths), the
+    Schur assembly (one-hot n^2; Hankel/sparse nnz^2; dense
+    4 n^3 m + m^2 n(n+1)/2), m^3/3 + 4 m^2 for the Schur factor and solves
+    and m^2 ns for the scalar block."""
+    m = model.m
+    f = m ** 3 / 3.0 + 4.0 * m * m + float(m) * m * model.ns
+    for n, A in zip(model.sides, model.A):
+        f += 28.0 * n ** 3
+        if A.nnz >= m * n * n // 2:
+            f += 4.0 * n ** 3 * m + float(m) * m * n * (n + 1) / 2.0
+        else:
+            f += float(A.nnz) ** 2
+    return f
+
+
+def _oracle_iterations(spec, seed, q):
+    sys.path[:0] = [ROOT, PKG]
+    from oracle import madsdp_oracle as o
+    model = instance_model(spec, seed)
+    s = o.Solver(model)
+    t = time.perf_counter()
+    s.initialize()
+    s.update_termination()
+    q.put(("init", time.perf_counter() - t))
+    while s.status == o.Status.REGULAR:
+        t = time.perf_counter()
+        s.iterate()
+        if s.status != o.Status.REGULAR:
+            break
+        s.update_termination()
+        q.put(("iter", time.perf_counter() - t))
+    q.put(("done", s.iter))
+
+
+def cpu_instance_sample(spec, seed, seconds):
+    """Iterations of the oracle on the same instance (all BLAS threads) for
+    about `seconds`; returns (seconds per iteration or None, iterations, init s)."""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    proc = ctx.Process(target=_oracle_iterations, args=(spec, seed, q))
+    proc.start()
+    t0 = time.perf_counter()
+    iters, init = [], None
+    while time.perf_counter() - t0 < seconds + 600:
+        try:
+            kind, v = q.get(timeout=1.0)
+        except Exception:
+            if not proc.is_alive():
+                break
+            if init is not None and time.perf_counter() - t0 > seconds:
+                break
+            continue
+        if kind == "init":
+            init = v
+            t0 = time.perf_counter()
+        elif kind == "iter":
+            iters.append(v)
+            if time.perf_counter() - t0 > seconds:
+                break
+        else:
+            break
+    proc.terminate()
+    proc.join(5)
+    return (statistics.mean(iters) if iters else None), len(iters), init
+
+
+def run_instance(args):
+    """One large problem per step on the whole GPU (msdp_solver)."""
+    import numpy as np
+    spec = INSTANCE_WORKLOADS[args.workload]
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_instance_sample(spec, args.seed, args.cpu_seconds)
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import madsdp_gpu as M
+    model = instance_model(spec, args.seed)
+    ctx = M.Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle, device=torch.device("cuda", 0))
+    solver = M.InstanceSolver(model, context=ctx)
+    for _ in range(args.warmup):
+        solver.solve()
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms, launches = [], solver.launch_count
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        solver.solve()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    clocks = sampler.stop()
+    launches = solver.launch_count - launches
+    st = solver.stats()
+    device_bytes = solver.device_bytes
+    solver.close()
+    # end to end: upload, solve, download through the public API
+    t = time.perf_counter()
+    e2 = M.InstanceSolver(model, context=ctx)
+    e2.solve()
+    X, y, x, z = e2.solution()
+    e2e_s = time.perf_counter() - t
+    h2d = sum(8 * n * n for n in model.sides) + sum(16 * A.nnz + 12 * A.nnz for A in model.A) + 8 * (
+        model.m + model.ns + model.m * model.ns)
+    d2h = sum(8 * n * n for n in model.sides) + 8 * (model.m + 2 * model.ns)
+    e2.close()
+    t_solve = statistics.mean(ms) / 1000.0
+    flops = instance_flops_per_iteration(model) * st["iter"]
+    fp64_peak = 1.25e3  # GB300 FP64 nominal, GFLOP/s
+    cpu_block = None
+    if cpu is not None:
+        per_it, nit, init = cpu
+        if per_it is not None:
+            est = (init or 0.0) + per_it * st["iter"]
+            cpu_block = {"value": 1.0 / est, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"oracle (NumPy/SciPy FP64, all BLAS threads) on the same instance: "
+                                   f"{nit} iterations timed, solve time = init + mean iteration x {st['iter']} GPU iterations"}
+        else:
+            cpu_block = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"oracle did not finish one iteration within {args.cpu_seconds:.0f} s"}
+    line = {
+        "metric": METRIC, "value": 1.0 / t_solve, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(ms), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, **{k: v for k, v in spec.items() if k != "kind"}, "seed": args.seed,
+                   "m": model.m, "components": "PrimalDual(NT, EigenStep, Mehrotra) + DenseCholesky, ScaledIdentity",
+                   "engine": "whole-GPU instance solver (cuBLAS/cuSOLVER dense algebra + own assembly/residual kernels)",
+                   "status": str(st["status"]), "iterations": st["iter"], "pobj": st["pobj"], "gap": st["gap"],
+                   "inf_pr": st["inf_pr"], "inf_du": st["inf_du"],
+                   "l2": f"{device_bytes / 2**20:.0f} MiB resident"},
+        "gpu_launches": launches // max(1, args.steps),
+        "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "fp64", "achieved": flops / t_solve / 1e9, "peak": fp64_peak, "unit": "GFLOP/s",
+                     "frac": flops / t_solve / 1e9 / fp64_peak, "traffic": None,
+                     "peak_kind": "nominal FP64 dense (no measured FP64 peak)",
+                     "note": "algorithmic flops of the iterations (model above) / solve time"},
+        "cpu_baseline": cpu_block,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
 
 
 # ----------------------------------------------------------------- clocks
@@ -272,13 +440,8 @@ def run_gpu(args):
     device_bytes = bm.device_bytes
     bm.close()
 
-    t_step = max(step_ms) if False else statistics.mean(step_ms)
-    if world > 1:
-        t = torch.tensor([sum(step_ms)], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    else:
-        total_ms = sum(step_ms)
+    from madsdp_gpu.distributed import max_over_ranks
+    total_ms = max_over_ranks(sum(step_ms))
     value = args.instances * world * args.steps / (total_ms / 1000.0)
     fp64_value = args.instances / (statistics.mean(s64) / 1000.0)
 
@@ -296,6 +459,22 @@ def run_gpu(args):
         be.close()
         e2e_times.append(time.perf_counter() - t0)
     e2e_value = args.instances / statistics.mean(e2e_times[1:] if len(e2e_times) > 1 else e2e_times)
+
+    # ---- served Poisson stream (continuous batching, real time)
+    serving = None
+    if args.serve_seconds > 0:
+        from madsdp_gpu.serving import Server, poisson_stream, serve_stream
+        stream = poisson_stream(args.serve_rate, args.serve_seconds, seed=args.seed + 17 + rank,
+                                sos_d=SERVE_MIX["sos_d"], maxcut_n=SERVE_MIX["maxcut_n"],
+                                dense_n=SERVE_MIX["dense_n"], dense_m=SERVE_MIX["dense_m"])
+        srv = Server(memory_budget_bytes=8 << 30, max_slots=4096, precision="mixed", context=ctx)
+        serving = serve_stream(srv, stream, iterations=args.serve_iterations, time_limit=600.0)
+        srv.close()
+        serving.update({"rate_per_s": args.serve_rate, "duration_s": args.serve_seconds,
+                        "iterations_per_wave": args.serve_iterations, "memory_budget_bytes": 8 << 30,
+                        "mix": "50%% SOS d~U%s, 30%% max-cut n~U%s p=4/n, 20%% dense one block n~U%s m<=min(%d, n(n+1)/2)"
+                               % (SERVE_MIX["sos_d"], SERVE_MIX["maxcut_n"], SERVE_MIX["dense_n"], SERVE_MIX["dense_m"]),
+                        "latency": "host clock, arrival to result available"})
 
     if rank != 0:
         return
@@ -331,7 +510,9 @@ def run_gpu(args):
             "workload": "sos_hankel_batch (4th workload: batched SOS SDPs)", "instances_per_gpu": args.instances,
             "d_range": [5, 63], "m": "2d+1", "ns": 2, "seed": args.seed,
             "components": "PrimalDual(NT, EigenStep, Mehrotra) + DenseCholesky, ScaledIdentity",
-            "precision": f"mixed (FP32 block algebra while max(inf_pr,inf_du,gap) > 1e-3, then FP64)",
+            "precision": "mixed: FP32 block algebra and Schur factor, each direction refined twice against the "
+                         "float64 primal defect; FP64 iterations after an FP32 failure, a short step or a rejected "
+                         "direction",
             "parallelism": f"one persistent launch, one CTA per instance; {world} GPU(s) x own instances",
             "l2": f"inputs and workspaces ({device_bytes / 2**20:.0f} MiB resident) larger than L2",
             "converged_1e-7": f"{sum(conv)}/{len(conv)}", "fp64_converged": f"{sum(conv64)}/{len(conv64)}",
@@ -340,6 +521,7 @@ def run_gpu(args):
             "fp32_iterations_mean": float(np.mean([s["iter_fp32"] for s in stm])),
             "fp64_gpu_solves_per_s": fp64_value, "mixed_over_fp64": value / world / fp64_value,
             "mixed_vs_fp64_max_rel_obj_diff": max(rel), "mixed_vs_oracle_max_rel_obj_diff": oracle_err,
+            "served_stream": serving,
         },
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -366,8 +548,17 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-iterations", type=int, default=2)
+    ap.add_argument("--workload", default="sos_batch", choices=["sos_batch", *INSTANCE_WORKLOADS])
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload != "sos_batch":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the default workload"}))
+            return
+        run_instance(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

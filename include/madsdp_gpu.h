@@ -161,7 +161,7 @@ int msdp_batch_destroy(msdp_batch* batch);
 /* Bytes of device memory the batch holds. */
 int64_t msdp_batch_device_bytes(const msdp_batch* batch);
 
-/* InitialPoint(X, y; x) of problem `prob` (src/components.jl:286-294); x may be NULL. */
+/* InitialPoint(X, y; x) of problem `prob` (src/components.jl:234-252); x may be NULL. */
 int msdp_batch_set_initial_point(msdp_batch* batch, int32_t prob, const double* const* X,
                                  const double* y, const double* x);
 /* Overwrite the iterate (X, S per block, y, x, z); NULL pointers keep the current value. */
@@ -211,6 +211,32 @@ enum msdp_block_matrix { MSDP_MAT_W = 0, MSDP_MAT_CORR = 1, MSDP_MAT_SI = 2, MSD
 int msdp_batch_get_profile(msdp_batch* batch, int32_t prob, double* out, int32_t capacity);
 const char* msdp_profile_field_name(int32_t index);
 
+/* ---- continuous-batching server ---------------------------------------------
+ * The serving loop of MadSDP's batched/served use (no counterpart in the
+ * reference, which solves one model per call): requests of any size are
+ * submitted at any time; each msdp_server_step admits pending requests in
+ * arrival order while their data and workspaces fit the memory budget,
+ * initializes them, advances every active request by `iterations`
+ * interior-point iterations in one persistent launch, and moves finished
+ * requests (stats and solution) to host memory, freeing their device memory
+ * for the next admissions.  All device memory is allocated at creation. */
+typedef struct msdp_server msdp_server;
+int msdp_server_create(msdp_context* ctx, const msdp_components* comp, const msdp_options* opt,
+                       int64_t memory_budget_bytes, int32_t max_slots, msdp_server** server);
+int msdp_server_destroy(msdp_server* server);
+/* Copies the problem; returns MSDP_ERR_TOO_LARGE if it can never fit. */
+int msdp_server_submit(msdp_server* server, const msdp_problem_desc* problem, int64_t* request_id);
+int msdp_server_step(msdp_server* server, int32_t iterations, int32_t* active, int32_t* completed);
+int msdp_server_counts(const msdp_server* server, int32_t* pending, int32_t* active, int64_t* completed);
+/* 1 while the request is not finished; 0 once its results are copied out
+ * (the request is then forgotten).  latency_s = finish - submit, host clock. */
+int msdp_server_result(msdp_server* server, int64_t request_id, msdp_stats* stats, double* const* X, double* y,
+                       double* x, double* z, double* latency_s);
+/* Ids of requests finished since the last call (up to `capacity`, oldest
+ * first); each id is reported once. */
+int msdp_server_finished(msdp_server* server, int64_t* ids, int32_t capacity, int32_t* count);
+int64_t msdp_server_launch_count(const msdp_server* server);
+
 /* ---- solve without allocating --------------------------------------------
  * msdp_solve_static has no counterpart in the reference.  It is for callers
  * that may not allocate device memory: a serving runtime or plugin host that
@@ -243,6 +269,34 @@ int msdp_solve_static(const msdp_problem_desc* problem, const msdp_components* c
 
 /* Number of kernel launches issued by this batch since creation. */
 int64_t msdp_batch_launch_count(const msdp_batch* batch);
+
+/* ---- one large problem on the whole GPU -------------------------------------
+ * MadSDPSolver + solve! (src/solver.jl:87-160, 385-396) for a single problem
+ * whose blocks or constraint count are too large for one thread block per
+ * problem (max-cut n = 2000, dense constraints with m = 2000, ...).  Each
+ * iteration runs as device-wide operations on the context's stream: dense
+ * products, Cholesky factorizations and symmetric eigendecompositions
+ * through cuBLAS/cuSOLVER, and this library's kernels for the Schur
+ * assembly of coordinate-list constraints, A(X), A*(y), residuals, NT
+ * scaling, correction and reductions.  Step lengths use exact eigenvalues.
+ * PrimalDual (NT or HKM; EigenStep or CholeskyBacktrack; Mehrotra or
+ * AdaptiveMu) with DenseCholesky in FP64; other components return
+ * MSDP_ERR_UNSUPPORTED.  All device memory is allocated at creation. */
+typedef struct msdp_solver msdp_solver;
+int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* problem, const msdp_components* comp,
+                       const msdp_options* opt, msdp_solver** solver);
+int msdp_solver_destroy(msdp_solver* solver);
+/* InitialPoint(X, y; x) (src/components.jl:234-252); x = NULL means ones. */
+int msdp_solver_set_initial_point(msdp_solver* solver, const double* const* X, const double* y, const double* x);
+/* initialize + iterate to termination; the status is in msdp_solver_get_stats. */
+int msdp_solver_solve(msdp_solver* solver);
+int msdp_solver_get_stats(const msdp_solver* solver, msdp_stats* out);
+int msdp_solver_get_solution(msdp_solver* solver, double* const* X, double* y, double* x, double* z);
+int msdp_solver_get_trajectory(const msdp_solver* solver, msdp_iter_record* out, int32_t capacity, int32_t* count);
+int64_t msdp_solver_device_bytes(const msdp_solver* solver);
+/* Launches of this library's own kernels (library calls not counted). */
+int64_t msdp_solver_launch_count(const msdp_solver* solver);
+const char* msdp_solver_last_error(const msdp_solver* solver);
 
 #ifdef __cplusplus
 }

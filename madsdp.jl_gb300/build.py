@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libmadsdp_gpu.so")
-UNITS = ["kernel_fp64.cu", "kernel_mixed.cu", "capi.cu", "noalloc.cu"]
+UNITS = ["kernel_fp64.cu", "kernel_mixed.cu", "capi.cu", "noalloc.cu", "server.cu", "instance.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -66,7 +66,7 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {cmd[-3]}")
-    link = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+    link = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lcublas", "-lcusolver"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         sys.stderr.write(" ".join(link) + "\n" + r.stdout + r.stderr)

@@ -339,7 +339,7 @@ int msdp_batch_create(msdp_context* ctx, const msdp_problem_desc* probs, int32_t
           prev_col = hecol[e];
         }
       }
-      bd.structure = hankel ? STRUCT_HANKEL : STRUCT_GENERAL;
+      bd.structure = choose_structure(hankel, n, m, nnz);
       // by position (counting sort, stable in constraint order)
       int64_t* pptr = hptr.data() + bd.posptr;
       for (int64_t e = 0; e < nnz; ++e) pptr[row[e] + col[e] * n + 1] += 1;

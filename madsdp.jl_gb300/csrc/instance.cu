@@ -1,0 +1,1243 @@
+// Whole-GPU solver for one large SDP (blocks of hundreds to thousands, m in
+// the thousands): every step of the interior-point iteration is a sequence
+// of device-wide operations on one stream.  Dense products, Cholesky
+// factorizations and symmetric eigendecompositions go to cuBLAS/cuSOLVER;
+// the Schur-complement assembly of sparse constraints, A(X), A*(y), the
+// residuals, the NT scaling arithmetic, the Mehrotra correction and every
+// reduction are kernels of this file.  The iteration restates
+// src/primal_dual.jl, src/step.jl, src/directions.jl, src/blocks.jl and
+// src/solver.jl (file:line at each step) with exact eigenvalues for the
+// step lengths.
+//
+// Constraint storage is chosen per block: coordinate lists (assembly cost
+// nnz^2 entry pairs: one-hot, Hankel, sparse) or dense n x n per constraint
+// (assembly by GEMMs: H = svec(G'A_jG) svec(G'A_kG)' for NT,
+// H_jk = <A_j, S^-1 A_k X> for HKM) when nnz^2 exceeds the dense cost.
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/madsdp_gpu.h"
+
+struct msdp_context;
+extern "C" void* msdp_context_stream(const msdp_context* ctx);
+
+namespace {
+
+constexpr double kEps = 2.220446049250313e-16;
+constexpr int kThreads = 256;
+constexpr int kRedBlocks = 304;
+constexpr int kSlots = 8192;
+constexpr int kInfos = 4096;
+
+inline int grid_for(int64_t n) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + kThreads - 1) / kThreads, 152 * 16));
+}
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// ------------------------------------------------------------------ kernels
+enum { RED_DOT = 0, RED_MAXABS, RED_MINRATIO, RED_NONFINITE, RED_SUM, RED_MIN };
+
+__device__ __forceinline__ double red_combine(int op, double a, double b) {
+  if (op == RED_MINRATIO || op == RED_MIN) return fmin(a, b);
+  if (op == RED_MAXABS) return fmax(a, b);
+  return a + b;
+}
+__device__ __forceinline__ double red_identity(int op) {
+  return (op == RED_MINRATIO || op == RED_MIN) ? INFINITY : 0.0;
+}
+
+// Block partials of a reduction over a[i * stride] (and b[i]); a fixed grid
+// and tree make the result independent of timing.
+__global__ void k_reduce(int op, int64_t n, int64_t stride, const double* __restrict__ a,
+                         const double* __restrict__ b, double* __restrict__ partial) {
+  double acc = red_identity(op);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double va = a[i * stride];
+    double v;
+    switch (op) {
+      case RED_DOT: v = va * b[i]; break;
+      case RED_MAXABS: v = fabs(va); break;
+      case RED_MINRATIO: { const double d = b[i]; v = d < 0.0 ? -va / d : INFINITY; break; }
+      case RED_NONFINITE: v = isfinite(va) ? 0.0 : 1.0; break;
+      case RED_MIN: v = isnan(va) ? -INFINITY : va; break;  // NaN counts as not positive
+      default: v = va;
+    }
+    acc = red_combine(op, acc, v);
+  }
+  __shared__ double sh[kThreads];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = kThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = red_combine(op, sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void k_reduce_final(int op, int np, const double* __restrict__ partial, double* __restrict__ out) {
+  __shared__ double sh[kThreads];
+  double acc = red_identity(op);
+  for (int i = threadIdx.x; i < np; i += kThreads) acc = red_combine(op, acc, partial[i]);
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = kThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = red_combine(op, sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+// out = a*A + b*B + c*C + d*D + e*E, left to right; absent terms skipped.
+__global__ void k_lin(int64_t N, double* __restrict__ out, double a, const double* A, double b, const double* B,
+                      double c, const double* Cc, double d, const double* D, double e, const double* E) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    double v = a * A[i];
+    if (B) v = v + b * B[i];
+    if (Cc) v = v + c * Cc[i];
+    if (D) v = v + d * D[i];
+    if (E) v = v + e * E[i];
+    out[i] = v;
+  }
+}
+
+// A = (A + A')/2 in place (src/blocks.jl:77-84).
+__global__ void k_sym(int n, double* A) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nn; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx % n), j = (int)(idx / n);
+    if (i > j) {
+      const double v = (A[idx] + A[j + (int64_t)i * n]) / 2;
+      A[idx] = v;
+      A[j + (int64_t)i * n] = v;
+    }
+  }
+}
+
+// out = sym(R - T)
+__global__ void k_sym_diff(int n, const double* R, const double* T, double* out) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nn; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx % n), j = (int)(idx / n);
+    if (i >= j) {
+      const int64_t t = j + (int64_t)i * n;
+      const double v = ((R[idx] - T[idx]) + (R[t] - T[t])) / 2;
+      out[idx] = v;
+      out[t] = v;
+    }
+  }
+}
+
+__global__ void k_lower_to_full(int n, double* A) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nn; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx % n), j = (int)(idx / n);
+    if (i < j) A[idx] = A[j + (int64_t)i * n];
+  }
+}
+
+// Lower Cholesky factor post-processing (src/blocks.jl:101-111): the upper
+// triangle is cleared and entries below eps^2 max|L_ii| are flushed to zero.
+__global__ void k_chol_post(int n, double* L, const double* maxdiag) {
+  const double tol = kEps * kEps * (*maxdiag);
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nn; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx % n), j = (int)(idx / n);
+    if (i < j || fabs(L[idx]) < tol) L[idx] = 0.0;
+  }
+}
+
+__global__ void k_add_diag(int n, double* A, int64_t lda, double v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) A[i + i * lda] += v;
+}
+
+__global__ void k_identity(int n, double* A, double v) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nn; idx += (int64_t)gridDim.x * blockDim.x)
+    A[idx] = (idx % n == idx / n) ? v : 0.0;
+}
+
+__global__ void k_fill(int64_t N, double* a, double v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
+}
+
+// D = sqrt(lambda), sc = sqrt(D) (src/directions.jl:55-60)
+__global__ void k_nt_scaling(int n, const double* lam, double* D, double* sc) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    D[i] = sqrt(lam[i]);
+    sc[i] = sqrt(D[i]);
+  }
+}
+
+// G[:, j] /= sc[j]
+__global__ void k_div_cols(int n, double* G, const double* sc) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nn; idx += (int64_t)gridDim.x * blockDim.x)
+    G[idx] /= sc[idx / n];
+}
+
+// out = diag(sc) V'
+__global__ void k_gi0(int n, const double* V, const double* sc, double* out) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nn; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx % n), j = (int)(idx / n);
+    out[idx] = V[j + (int64_t)i * n] * sc[i];
+  }
+}
+
+// out = -(M + M') ./ (D_i + D_j)  (src/directions.jl:90-100)
+__global__ void k_rnt(int n, const double* M, const double* D, double* out) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nn; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx % n), j = (int)(idx / n);
+    out[idx] = -(M[idx] + M[j + (int64_t)i * n]) / (D[i] + D[j]);
+  }
+}
+
+// out[r, c] = A[r, c] * w[c]  (rows x cols, column-major)
+__global__ void k_scale_cols(int64_t rows, int64_t cols, const double* A, const double* w, double* out) {
+  const int64_t N = rows * cols;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < N; idx += (int64_t)gridDim.x * blockDim.x)
+    out[idx] = A[idx] * w[idx / rows];
+}
+
+// Scalar block helpers (src/step.jl:63-124, 128-136)
+__global__ void k_inv(int ns, const double* z, double* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) out[i] = 1.0 / z[i];
+}
+__global__ void k_mul(int ns, const double* a, const double* b, double* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) out[i] = a[i] * b[i];
+}
+// v = x - mu zinv + x zinv Rd_lin [- corr]
+__global__ void k_rhs_lin(int ns, double mu, const double* x, const double* zinv, const double* rdl, const double* corr,
+                          double* v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+    double t = x[i] - mu * zinv[i] + x[i] * zinv[i] * rdl[i];
+    if (corr) t = t - corr[i];
+    v[i] = t;
+  }
+}
+// delz = Rd_lin - C'dy ; delx = mu zinv - x - x zinv delz [+ corr]
+__global__ void k_dir_lin(int ns, double mu, const double* rdl, const double* ctdy, const double* x, const double* zinv,
+                          const double* corr, double* delz, double* delx) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+    const double dz = rdl[i] - ctdy[i];
+    double dx = mu * zinv[i] - x[i] - x[i] * zinv[i] * dz;
+    if (corr) dx = dx + corr[i];
+    delz[i] = dz;
+    delx[i] = dx;
+  }
+}
+__global__ void k_corr_lin(int ns, const double* dx, const double* dz, const double* zinv, double* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x)
+    out[i] = -dx[i] * dz[i] * zinv[i];
+}
+// (x + a dx)(z + b dz)
+__global__ void k_aff_lin(int ns, double a, double b, const double* x, const double* dx, const double* z,
+                          const double* dz, double* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x)
+    out[i] = (x[i] + a * dx[i]) * (z[i] + b * dz[i]);
+}
+
+// ---- coordinate-list constraints of one block
+// out[j] (+)= sum_{e in j} v_e X[r_e, c_e]
+__global__ void k_jprod(int m, const int64_t* __restrict__ conptr, const int32_t* __restrict__ row,
+                        const int32_t* __restrict__ col, const double* __restrict__ val, int n,
+                        const double* __restrict__ X, double* __restrict__ out, int accumulate) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int64_t q = conptr[j]; q < conptr[j + 1]; ++q) s += val[q] * X[row[q] + (int64_t)col[q] * n];
+    out[j] = accumulate ? out[j] + s : s;
+  }
+}
+
+// out[p] = sum_{e at position p} v_e y[con_e]
+__global__ void k_jtprod(int64_t nn, const int64_t* __restrict__ posptr, const int32_t* __restrict__ pcon,
+                         const double* __restrict__ pval, const double* __restrict__ y, double* __restrict__ out) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nn; p += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int64_t q = posptr[p]; q < posptr[p + 1]; ++q) s += pval[q] * y[pcon[q]];
+    out[p] = s;
+  }
+}
+
+// H[j, k] += <A_j, L A_k R> for j >= k: sum over entry pairs
+// v_e v_f L[r_e, r_f] R[c_f, c_e] (the semantics of LowRankOpt's
+// schur_complement!, src/solver.jl:30-31,117-118).
+__global__ void k_schur_pairs(int m, const int64_t* __restrict__ conptr, const int32_t* __restrict__ row,
+                              const int32_t* __restrict__ col, const double* __restrict__ val, int n,
+                              const double* __restrict__ L, const double* __restrict__ R, double* __restrict__ H) {
+  const int64_t npairs = (int64_t)m * (m + 1) / 2;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npairs; p += (int64_t)gridDim.x * blockDim.x) {
+    int64_t j = (int64_t)((sqrt(8.0 * (double)p + 1.0) - 1.0) / 2.0);
+    while (j * (j + 1) / 2 > p) --j;
+    while ((j + 1) * (j + 2) / 2 <= p) ++j;
+    const int64_t k = p - j * (j + 1) / 2;
+    double s = 0.0;
+    for (int64_t e = conptr[j]; e < conptr[j + 1]; ++e) {
+      const int re = row[e], ce = col[e];
+      const double ve = val[e];
+      double t = 0.0;
+      for (int64_t f = conptr[k]; f < conptr[k + 1]; ++f)
+        t += val[f] * L[re + (int64_t)row[f] * n] * R[col[f] + (int64_t)ce * n];
+      s += ve * t;
+    }
+    H[j + k * (int64_t)m] += s;
+  }
+}
+
+// ------------------------------------------------------------------ host state
+struct Blk {
+  int n = 0;
+  bool dense = false;
+  int64_t nnz = 0;
+  double cnorm = 0.0;
+  bool rd_nonzero = true;
+  double *C = nullptr, *X = nullptr, *S = nullptr, *Rd = nullptr, *Ls = nullptr, *Si = nullptr, *Lx = nullptr;
+  double *W = nullptr, *G = nullptr, *Gi = nullptr, *dX = nullptr, *dS = nullptr, *corr = nullptr, *ERd = nullptr;
+  double *T1 = nullptr, *T2 = nullptr, *T3 = nullptr;
+  double *lam = nullptr, *D = nullptr, *sc = nullptr, *w = nullptr;
+  int64_t *conptr = nullptr, *posptr = nullptr;
+  int32_t *erow = nullptr, *ecol = nullptr, *pcon = nullptr;
+  double *eval = nullptr, *pval = nullptr;
+  double* Aall = nullptr;  // dense: n x (n m), column j*n.. of A_j
+};
+
+}  // namespace
+
+struct msdp_solver {
+  msdp_context* ctx = nullptr;
+  cudaStream_t st = nullptr;
+  cublasHandle_t cb = nullptr;
+  cusolverDnHandle_t cs = nullptr;
+  msdp_components comp{};
+  msdp_options opt{};
+  int m = 0, ns = 0, nb = 0;
+  std::vector<Blk> B;
+  std::vector<void*> allocs;
+  int64_t bytes = 0;
+  double *b = nullptr, *dlin = nullptr, *Clin = nullptr, *Cw = nullptr;
+  double *y = nullptr, *dy = nullptr, *Rp = nullptr, *h = nullptr, *acc = nullptr;
+  double *x = nullptr, *z = nullptr, *dx = nullptr, *dz = nullptr, *Rdlin = nullptr, *zinv = nullptr;
+  double *corrlin = nullptr, *vlin = nullptr, *ctv = nullptr, *wlin = nullptr;
+  double *H = nullptr, *H0 = nullptr, *Tb = nullptr, *Bb = nullptr;
+  double* work = nullptr;
+  int lwork = 0;
+  int* dinfo = nullptr;
+  double *partial = nullptr, *slots = nullptr;
+  double* hslots = nullptr;
+  int* hinfo = nullptr;
+  int nslot = 0, ninfo = 0;
+  double bnorm = 0.0, dnorm = 0.0, cmax = 0.0;
+  // user initial point
+  bool has_ip = false;
+  std::vector<std::vector<double>> ipX;
+  std::vector<double> ipy, ipx;
+  // iteration state
+  int status = MSDP_INITIAL, iter = 0;
+  double mu = 0, sigma = 0, alpha = 0, beta = 0, inf_pr = 0, inf_du = 0, gap = 0, pobj = 0, dobj = 0;
+  double t0 = 0, solve_s = 0;
+  std::vector<msdp_iter_record> traj;
+  int64_t launches = 0;
+  int fail = 0;  // first library/CUDA error seen
+  std::string err;
+};
+
+namespace {
+
+using S = msdp_solver;
+
+#define LAUNCH(s, kern, n, ...)                                          \
+  do {                                                                   \
+    kern<<<grid_for(n), kThreads, 0, (s)->st>>>(__VA_ARGS__);            \
+    (s)->launches += 1;                                                  \
+  } while (0)
+
+void note(S* s, bool ok, const char* what) {
+  if (!ok && !s->fail) {
+    s->fail = MSDP_ERR_CUDA;
+    s->err = what;
+  }
+}
+#define CB(s, call) note(s, (call) == CUBLAS_STATUS_SUCCESS, #call)
+#define CS(s, call) note(s, (call) == CUSOLVER_STATUS_SUCCESS, #call)
+#define CU(s, call) note(s, (call) == cudaSuccess, #call)
+
+template <class T>
+T* dalloc(S* s, int64_t count) {
+  void* p = nullptr;
+  if (count <= 0) count = 1;
+  if (cudaMalloc(&p, sizeof(T) * count) != cudaSuccess) return nullptr;
+  s->allocs.push_back(p);
+  s->bytes += sizeof(T) * count;
+  return (T*)p;
+}
+
+// ---- reductions into slots
+int reduce(S* s, int op, int64_t n, const double* a, const double* b = nullptr, int64_t stride = 1) {
+  const int slot = s->nslot++;
+  if (n <= 0) {
+    LAUNCH(s, k_fill, 1, 1, s->slots + slot, (op == RED_MINRATIO || op == RED_MIN) ? INFINITY : 0.0);
+    return slot;
+  }
+  k_reduce<<<kRedBlocks, kThreads, 0, s->st>>>(op, n, stride, a, b, s->partial);
+  k_reduce_final<<<1, kThreads, 0, s->st>>>(op, kRedBlocks, s->partial, s->slots + slot);
+  s->launches += 2;
+  return slot;
+}
+
+int copy_slot(S* s, const double* src) {
+  const int slot = s->nslot++;
+  CU(s, cudaMemcpyAsync(s->slots + slot, src, sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+  return slot;
+}
+
+// Bring every slot and info written since the last fetch to the host.
+bool fetch(S* s) {
+  if (s->nslot) CU(s, cudaMemcpyAsync(s->hslots, s->slots, sizeof(double) * s->nslot, cudaMemcpyDeviceToHost, s->st));
+  if (s->ninfo) CU(s, cudaMemcpyAsync(s->hinfo, s->dinfo, sizeof(int) * s->ninfo, cudaMemcpyDeviceToHost, s->st));
+  CU(s, cudaStreamSynchronize(s->st));
+  return !s->fail;
+}
+void reset_slots(S* s) { s->nslot = 0; s->ninfo = 0; }
+int next_info(S* s) { return s->ninfo < kInfos ? s->ninfo++ : kInfos - 1; }
+
+// ---- dense linear algebra
+void gemm(S* s, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k, double alpha, const double* A, int lda,
+          const double* Bm, int ldb, double beta, double* C, int ldc) {
+  CB(s, cublasDgemm(s->cb, ta, tb, m, n, k, &alpha, A, lda, Bm, ldb, &beta, C, ldc));
+}
+
+// potrf of the lower triangle in place; returns the info index
+int potrf(S* s, int n, double* A, int lda) {
+  const int k = next_info(s);
+  CS(s, cusolverDnDpotrf(s->cs, CUBLAS_FILL_MODE_LOWER, n, A, lda, s->work, s->lwork, s->dinfo + k));
+  return k;
+}
+
+struct CholCheck {
+  int info, nonfinite;
+};
+
+// Lower Cholesky factor of sym(M) with the flush (src/blocks.jl:94-113);
+// success is known after fetch: info == 0 and no non-finite entry.
+CholCheck chol_factor(S* s, int n, const double* M, double* L) {
+  CU(s, cudaMemcpyAsync(L, M, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, s->st));
+  LAUNCH(s, k_sym, (int64_t)n * n, n, L);
+  CholCheck c;
+  c.nonfinite = reduce(s, RED_NONFINITE, (int64_t)n * n, L);
+  c.info = potrf(s, n, L, n);
+  const int md = reduce(s, RED_MAXABS, n, L, nullptr, n + 1);
+  LAUNCH(s, k_chol_post, (int64_t)n * n, n, L, s->slots + md);
+  return c;
+}
+bool chol_ok(S* s, const CholCheck& c) { return s->hinfo[c.info] == 0 && s->hslots[c.nonfinite] == 0.0; }
+
+// ---- constraint operators of one block
+void jprod(S* s, Blk& b, const double* X, double* out, bool accumulate) {
+  if (b.dense) {
+    const double one = 1.0, beta = accumulate ? 1.0 : 0.0;
+    CB(s, cublasDgemv(s->cb, CUBLAS_OP_T, b.n * b.n, s->m, &one, b.Aall, b.n * b.n, X, 1, &beta, out, 1));
+  } else {
+    LAUNCH(s, k_jprod, s->m, s->m, b.conptr, b.erow, b.ecol, b.eval, b.n, X, out, accumulate ? 1 : 0);
+  }
+}
+
+void jtprod(S* s, Blk& b, const double* yv, double* out) {
+  const int64_t nn = (int64_t)b.n * b.n;
+  if (b.dense) {
+    const double one = 1.0, zero = 0.0;
+    CB(s, cublasDgemv(s->cb, CUBLAS_OP_N, b.n * b.n, s->m, &one, b.Aall, b.n * b.n, yv, 1, &zero, out, 1));
+  } else {
+    LAUNCH(s, k_jtprod, nn, nn, b.posptr, b.pcon, b.pval, yv, out);
+  }
+}
+
+bool is_nt(const S* s) { return s->comp.direction == MSDP_NT; }
+
+// E(M): NT  W M W,  HKM  sym(X M S^-1)  (src/directions.jl:80-84,116-120)
+void apply_E(S* s, Blk& b, const double* M, double* out) {
+  const int n = b.n;
+  if (is_nt(s)) {
+    gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.W, n, M, n, 0.0, b.T3, n);
+    gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.T3, n, b.W, n, 0.0, out, n);
+  } else {
+    gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.X, n, M, n, 0.0, b.T3, n);
+    gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.T3, n, b.Si, n, 0.0, out, n);
+  }
+  LAUNCH(s, k_sym, (int64_t)n * n, n, out);
+}
+
+// ---- residuals and termination (src/step.jl:12-47, src/primal_dual.jl:123-134)
+bool update_residuals(S* s) {
+  reset_slots(s);
+  const int m = s->m, ns = s->ns;
+  if (m) CU(s, cudaMemsetAsync(s->acc, 0, sizeof(double) * m, s->st));
+  for (auto& b : s->B) jprod(s, b, b.X, s->acc, true);
+  if (ns && m) {
+    const double one = 1.0;
+    CB(s, cublasDgemv(s->cb, CUBLAS_OP_N, m, ns, &one, s->Clin, m, s->x, 1, &one, s->acc, 1));
+  }
+  if (m) LAUNCH(s, k_lin, m, m, s->Rp, 1.0, s->b, -1.0, s->acc, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+  std::vector<int> rmax(s->nb);
+  for (int i = 0; i < s->nb; ++i) {
+    Blk& b = s->B[i];
+    const int64_t nn = (int64_t)b.n * b.n;
+    jtprod(s, b, s->y, b.T1);
+    LAUNCH(s, k_lin, nn, nn, b.Rd, 1.0, b.C, -1.0, b.S, -1.0, b.T1, 0.0, nullptr, 0.0, nullptr);
+    rmax[i] = reduce(s, RED_MAXABS, nn, b.Rd);
+  }
+  if (ns) {
+    const double one = 1.0, zero = 0.0;
+    if (m) CB(s, cublasDgemv(s->cb, CUBLAS_OP_T, m, ns, &one, s->Clin, m, s->y, 1, &zero, s->ctv, 1));
+    else CU(s, cudaMemsetAsync(s->ctv, 0, sizeof(double) * ns, s->st));
+    LAUNCH(s, k_lin, ns, ns, s->Rdlin, 1.0, s->dlin, -1.0, s->z, -1.0, s->ctv, 0.0, nullptr, 0.0, nullptr);
+  }
+  if (!fetch(s)) return false;
+  for (int i = 0; i < s->nb; ++i)
+    s->B[i].rd_nonzero = s->hslots[rmax[i]] > 100.0 * kEps * std::max(1.0, s->B[i].cnorm);
+  return true;
+}
+
+int nu(const S* s) {
+  int v = s->ns;
+  for (const auto& b : s->B) v += b.n;
+  return v;
+}
+
+bool total_complementarity(S* s, double* out) {
+  reset_slots(s);
+  std::vector<int> sl;
+  for (auto& b : s->B) sl.push_back(reduce(s, RED_DOT, (int64_t)b.n * b.n, b.X, b.S));
+  const int lin = s->ns ? reduce(s, RED_DOT, s->ns, s->x, s->z) : -1;
+  if (!fetch(s)) return false;
+  double v = 0.0;
+  for (int k : sl) v += s->hslots[k];
+  if (lin >= 0) v += s->hslots[lin];
+  *out = v;
+  return true;
+}
+
+bool update_termination(S* s) {
+  reset_slots(s);
+  std::vector<int> cx, rd;
+  for (auto& b : s->B) {
+    cx.push_back(reduce(s, RED_DOT, (int64_t)b.n * b.n, b.C, b.X));
+    rd.push_back(reduce(s, RED_MAXABS, (int64_t)b.n * b.n, b.Rd));
+  }
+  const int dx = s->ns ? reduce(s, RED_DOT, s->ns, s->dlin, s->x) : -1;
+  const int rdl = s->ns ? reduce(s, RED_MAXABS, s->ns, s->Rdlin) : -1;
+  const int by = reduce(s, RED_DOT, s->m, s->b, s->y);
+  const int rp = reduce(s, RED_MAXABS, s->m, s->Rp);
+  if (!fetch(s)) return false;
+  double pobj = 0.0;
+  for (int k : cx) pobj += s->hslots[k];
+  if (dx >= 0) pobj += s->hslots[dx];
+  const double dobj = s->hslots[by];
+  s->pobj = pobj;
+  s->dobj = dobj;
+  s->inf_pr = s->hslots[rp] / std::max(1.0, s->bnorm);
+  double r = 0.0, cn = s->cmax;
+  for (int k : rd) r = std::max(r, s->hslots[k]);
+  if (s->ns) {
+    r = std::max(r, s->hslots[rdl]);
+    cn = std::max(cn, s->dnorm);
+  }
+  s->inf_du = r / std::max(1.0, cn);
+  s->gap = std::fabs(pobj - dobj) / std::max(1.0, std::fabs(pobj) + std::fabs(dobj));
+  const bool converged = std::max(std::max(s->inf_pr, s->inf_du), s->gap) <= s->opt.tol;
+  if (converged) s->status = MSDP_SOLVE_SUCCEEDED;
+  else if (s->iter >= s->opt.max_iter) s->status = MSDP_MAXIMUM_ITERATIONS_EXCEEDED;
+  else if (now_s() - s->t0 >= s->opt.max_wall_time) s->status = MSDP_MAXIMUM_WALLTIME_EXCEEDED;
+  if (s->status == MSDP_REGULAR && s->mu < s->opt.mu_min) s->status = MSDP_SEARCH_DIRECTION_BECOMES_TOO_SMALL;
+  msdp_iter_record rec{};
+  rec.iter = s->iter; rec.pobj = pobj; rec.dobj = dobj; rec.inf_pr = s->inf_pr; rec.inf_du = s->inf_du;
+  rec.gap = s->gap; rec.mu = s->mu; rec.alpha = s->alpha; rec.beta = s->beta; rec.phase = 1.0;
+  s->traj.push_back(rec);
+  return true;
+}
+
+// ---- prepare (src/primal_dual.jl:29-37, src/directions.jl:45-75, src/blocks.jl:94-130)
+bool prepare(S* s, bool* ok) {
+  reset_slots(s);
+  const bool need_lx = is_nt(s) || s->comp.step == MSDP_EIGEN_STEP;
+  std::vector<CholCheck> cs_, cx_;
+  std::vector<int> lam0;
+  for (auto& b : s->B) {
+    const int n = b.n;
+    const int64_t nn = (int64_t)n * n;
+    cs_.push_back(chol_factor(s, n, b.S, b.Ls));
+    // S^-1 from the factor (potri on a copy, lower to full)
+    CU(s, cudaMemcpyAsync(b.Si, b.Ls, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s->st));
+    const int k = next_info(s);
+    CS(s, cusolverDnDpotri(s->cs, CUBLAS_FILL_MODE_LOWER, n, b.Si, n, s->work, s->lwork, s->dinfo + k));
+    LAUNCH(s, k_lower_to_full, nn, n, b.Si);
+    if (need_lx) cx_.push_back(chol_factor(s, n, b.X, b.Lx));
+    if (is_nt(s)) {
+      // M = Ls' Lx ; N = M'M ; eig(N) = V diag(lam) V'
+      gemm(s, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, 1.0, b.Ls, n, b.Lx, n, 0.0, b.T1, n);
+      const double one = 1.0, zero = 0.0;
+      CB(s, cublasDsyrk(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, n, n, &one, b.T1, n, &zero, b.T2, n));
+      const int ke = next_info(s);
+      CS(s, cusolverDnDsyevd(s->cs, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, b.T2, n, b.lam, s->work,
+                             s->lwork, s->dinfo + ke));
+      lam0.push_back(copy_slot(s, b.lam));
+      LAUNCH(s, k_nt_scaling, n, n, b.lam, b.D, b.sc);
+      // G = Lx V diag(sc)^-1 ; Gi = diag(sc) V' Lx^-1 ; W = G G'
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.Lx, n, b.T2, n, 0.0, b.G, n);
+      LAUNCH(s, k_div_cols, nn, n, b.G, b.sc);
+      LAUNCH(s, k_gi0, nn, n, b.T2, b.sc, b.Gi);
+      CB(s, cublasDtrsm(s->cb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                        b.Lx, n, b.Gi, n));
+      CB(s, cublasDsyrk(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, n, &one, b.G, n, &zero, b.W, n));
+      LAUNCH(s, k_lower_to_full, nn, n, b.W);
+    }
+  }
+  if (s->ns) LAUNCH(s, k_inv, s->ns, s->ns, s->z, s->zinv);
+  if (!fetch(s)) return false;
+  *ok = true;
+  for (size_t i = 0; i < cs_.size(); ++i) *ok = *ok && chol_ok(s, cs_[i]);
+  for (size_t i = 0; i < cx_.size(); ++i) *ok = *ok && chol_ok(s, cx_[i]);
+  for (int k : lam0) *ok = *ok && s->hslots[k] > 0.0;
+  if (*ok) {
+    // E(Rd) is fixed for the iteration: computed once for rhs and directions
+    for (auto& b : s->B)
+      if (b.rd_nonzero) apply_E(s, b, b.Rd, b.ERd);
+  }
+  return !s->fail;
+}
+
+// H = sum_i <A_ij, L_i A_ik R_i> + C_lin diag(x/z) C_lin' (lower triangle)
+void schur_complement(S* s, double* H) {
+  const int m = s->m;
+  CU(s, cudaMemsetAsync(H, 0, sizeof(double) * m * m, s->st));
+  const double one = 1.0, zero = 0.0;
+  for (auto& b : s->B) {
+    const int n = b.n;
+    const double* L = is_nt(s) ? b.W : b.Si;
+    const double* R = is_nt(s) ? b.W : b.X;
+    if (!b.dense) {
+      LAUNCH(s, k_schur_pairs, (int64_t)m * (m + 1) / 2, m, b.conptr, b.erow, b.ecol, b.eval, n, L, R, H);
+    } else if (is_nt(s)) {
+      // B_j = G' A_j G ; H += svec-free Gram matrix of the B_j
+      gemm(s, CUBLAS_OP_T, CUBLAS_OP_N, n, n * m, n, 1.0, b.G, n, b.Aall, n, 0.0, s->Tb, n);
+      CB(s, cublasDgemmStridedBatched(s->cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, s->Tb, n, (long long)n * n, b.G,
+                                      n, 0, &zero, s->Bb, n, (long long)n * n, m));
+      CB(s, cublasDsyrk(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, m, n * n, &one, s->Bb, n * n, &one, H, m));
+    } else {
+      // T_k = S^-1 A_k X ; H_jk += <A_j, T_k>
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n * m, n, 1.0, b.Si, n, b.Aall, n, 0.0, s->Tb, n);
+      CB(s, cublasDgemmStridedBatched(s->cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, s->Tb, n, (long long)n * n, b.X,
+                                      n, 0, &zero, s->Bb, n, (long long)n * n, m));
+      gemm(s, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n * n, 1.0, b.Aall, n * n, s->Bb, n * n, 1.0, H, m);
+    }
+  }
+  if (s->ns && m) {
+    LAUNCH(s, k_mul, s->ns, s->ns, s->x, s->zinv, s->wlin);
+    LAUNCH(s, k_scale_cols, (int64_t)m * s->ns, m, s->ns, s->Clin, s->wlin, s->Cw);
+    gemm(s, CUBLAS_OP_N, CUBLAS_OP_T, m, m, s->ns, 1.0, s->Cw, m, s->Clin, m, 1.0, H, m);
+  }
+}
+
+// Regularization retry loop (src/solver.jl:299-314, src/schur_solvers.jl:15-19)
+bool factorize_schur(S* s, bool* ok) {
+  const int m = s->m;
+  *ok = false;
+  if (m == 0) { *ok = true; return true; }
+  schur_complement(s, s->H0);
+  double reg = s->opt.regularize_schur;
+  for (int t = 0; t < s->opt.max_schur_reg; ++t) {
+    reset_slots(s);
+    CU(s, cudaMemcpyAsync(s->H, s->H0, sizeof(double) * m * m, cudaMemcpyDeviceToDevice, s->st));
+    if (reg > 0) LAUNCH(s, k_add_diag, m, m, s->H, (int64_t)m, reg);
+    const int nf = reduce(s, RED_NONFINITE, (int64_t)m * m, s->H);
+    const int k = potrf(s, m, s->H, m);
+    if (!fetch(s)) return false;
+    if (s->hinfo[k] == 0 && s->hslots[nf] == 0.0) { *ok = true; return true; }
+    reg = reg == 0.0 ? 1e-12 : 10.0 * reg;
+  }
+  return true;
+}
+
+// ---- directions (src/step.jl:63-124)
+void solve_directions(S* s, double mu, bool corrected) {
+  const int m = s->m, ns = s->ns;
+  const double one = 1.0, zero = 0.0;
+  // rhs
+  if (m) CU(s, cudaMemcpyAsync(s->h, s->Rp, sizeof(double) * m, cudaMemcpyDeviceToDevice, s->st));
+  for (auto& b : s->B) {
+    const int64_t nn = (int64_t)b.n * b.n;
+    LAUNCH(s, k_lin, nn, nn, b.T1, 1.0, b.X, -mu, b.Si, 1.0, b.rd_nonzero ? b.ERd : nullptr, -1.0,
+           corrected ? b.corr : nullptr, 0.0, nullptr);
+    jprod(s, b, b.T1, s->h, true);
+  }
+  if (ns && m) {
+    LAUNCH(s, k_rhs_lin, ns, ns, mu, s->x, s->zinv, s->Rdlin, corrected ? s->corrlin : nullptr, s->vlin);
+    CB(s, cublasDgemv(s->cb, CUBLAS_OP_N, m, ns, &one, s->Clin, m, s->vlin, 1, &one, s->h, 1));
+  }
+  // dely = H^-1 h
+  if (m) {
+    CU(s, cudaMemcpyAsync(s->dy, s->h, sizeof(double) * m, cudaMemcpyDeviceToDevice, s->st));
+    CB(s, cublasDtrsv(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, m, s->H, m, s->dy, 1));
+    CB(s, cublasDtrsv(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, m, s->H, m, s->dy, 1));
+  }
+  // directions
+  for (auto& b : s->B) {
+    const int64_t nn = (int64_t)b.n * b.n;
+    jtprod(s, b, s->dy, b.T1);
+    LAUNCH(s, k_sym_diff, nn, b.n, b.Rd, b.T1, b.dS);
+    apply_E(s, b, b.T1, b.T2);
+    LAUNCH(s, k_lin, nn, nn, b.dX, mu, b.Si, -1.0, b.X, 1.0, b.T2, -1.0, b.rd_nonzero ? b.ERd : nullptr, 1.0,
+           corrected ? b.corr : nullptr);
+    LAUNCH(s, k_sym, nn, b.n, b.dX);
+  }
+  if (ns) {
+    if (m) CB(s, cublasDgemv(s->cb, CUBLAS_OP_T, m, ns, &one, s->Clin, m, s->dy, 1, &zero, s->ctv, 1));
+    else CU(s, cudaMemsetAsync(s->ctv, 0, sizeof(double) * ns, s->st));
+    LAUNCH(s, k_dir_lin, ns, ns, mu, s->Rdlin, s->ctv, s->x, s->zinv, corrected ? s->corrlin : nullptr, s->dz, s->dx);
+  }
+}
+
+// ---- Mehrotra correction (src/step.jl:128-136, src/directions.jl:90-100,123-127)
+void correction(S* s) {
+  for (auto& b : s->B) {
+    const int n = b.n;
+    const int64_t nn = (int64_t)n * n;
+    if (is_nt(s)) {
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.Gi, n, b.dX, n, 0.0, b.T1, n);
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.T1, n, b.dS, n, 0.0, b.T2, n);
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.T2, n, b.G, n, 0.0, b.T1, n);
+      LAUNCH(s, k_rnt, nn, n, b.T1, b.D, b.T2);
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.G, n, b.T2, n, 0.0, b.T1, n);
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_T, n, n, n, 1.0, b.T1, n, b.G, n, 0.0, b.corr, n);
+    } else {
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.dX, n, b.dS, n, 0.0, b.T1, n);
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, -1.0, b.T1, n, b.Si, n, 0.0, b.corr, n);
+    }
+    LAUNCH(s, k_sym, nn, n, b.corr);
+  }
+  if (s->ns) LAUNCH(s, k_corr_lin, s->ns, s->ns, s->dx, s->dz, s->zinv, s->corrlin);
+}
+
+// ---- step lengths (src/step.jl:148-228)
+// slot of lambda_min(L^-1 D L^-T) (src/step.jl:150-163)
+int eigmin_congruence(S* s, Blk& b, const double* L, const double* D) {
+  const int n = b.n;
+  const double one = 1.0;
+  CU(s, cudaMemcpyAsync(b.T1, D, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, s->st));
+  CB(s, cublasDtrsm(s->cb, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one, L, n,
+                    b.T1, n));
+  CB(s, cublasDtrsm(s->cb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, n, &one, L,
+                    n, b.T1, n));
+  LAUNCH(s, k_sym, (int64_t)n * n, n, b.T1);
+  const int k = next_info(s);
+  CS(s, cusolverDnDsyevd(s->cs, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_LOWER, n, b.T1, n, b.w, s->work, s->lwork,
+                         s->dinfo + k));
+  return copy_slot(s, b.w);
+}
+
+double eigen_step(double lam, double tau) { return lam > -std::sqrt(kEps) ? 1.0 : std::min(1.0, -tau / lam); }
+
+// CholeskyBacktrack (src/step.jl:202-221)
+bool backtrack(S* s, bool primal, double* out) {
+  double a = 1.0;
+  const double shrink = s->comp.shrink, boundary = s->comp.boundary;
+  for (auto& b : s->B) {
+    const int64_t nn = (int64_t)b.n * b.n;
+    const double* Xv = primal ? b.X : b.S;
+    const double* dXv = primal ? b.dX : b.dS;
+    for (;;) {
+      reset_slots(s);
+      LAUNCH(s, k_lin, nn, nn, b.T1, 1.0, Xv, a, dXv, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+      const int nf = reduce(s, RED_NONFINITE, nn, b.T1);
+      const int k = potrf(s, b.n, b.T1, b.n);
+      if (!fetch(s)) return false;
+      if (s->hinfo[k] == 0 && s->hslots[nf] == 0.0) break;
+      a *= shrink;
+      if (a < kEps) { *out = 0.0; return true; }
+    }
+  }
+  if (a != 1.0) a *= boundary;
+  if (s->ns) {
+    reset_slots(s);
+    const int r = primal ? reduce(s, RED_MINRATIO, s->ns, s->x, s->dx) : reduce(s, RED_MINRATIO, s->ns, s->z, s->dz);
+    if (!fetch(s)) return false;
+    a = std::min(a, boundary * s->hslots[r]);
+  }
+  *out = a;
+  return true;
+}
+
+bool step_lengths(S* s, double* a_out, double* b_out) {
+  if (s->comp.step == MSDP_CHOLESKY_BACKTRACK)
+    return backtrack(s, true, a_out) && backtrack(s, false, b_out);
+  reset_slots(s);
+  std::vector<int> lx, ls;
+  for (auto& b : s->B) {
+    lx.push_back(eigmin_congruence(s, b, b.Lx, b.dX));
+    ls.push_back(eigmin_congruence(s, b, b.Ls, b.dS));
+  }
+  const int rx = s->ns ? reduce(s, RED_MINRATIO, s->ns, s->x, s->dx) : -1;
+  const int rz = s->ns ? reduce(s, RED_MINRATIO, s->ns, s->z, s->dz) : -1;
+  if (!fetch(s)) return false;
+  double a = 1.0, bt = 1.0;
+  const double tau = s->comp.tau;
+  for (size_t i = 0; i < lx.size(); ++i) {
+    a = std::min(a, eigen_step(s->hslots[lx[i]], tau));
+    bt = std::min(bt, eigen_step(s->hslots[ls[i]], tau));
+  }
+  if (s->ns) {
+    a = std::min(a, tau * s->hslots[rx]);
+    bt = std::min(bt, tau * s->hslots[rz]);
+  }
+  *a_out = a;
+  *b_out = bt;
+  return true;
+}
+
+// src/step.jl:231-243
+bool affine_complementarity(S* s, double a, double bt, double* out) {
+  reset_slots(s);
+  std::vector<int> sl;
+  for (auto& b : s->B) {
+    const int64_t nn = (int64_t)b.n * b.n;
+    sl.push_back(reduce(s, RED_DOT, nn, b.X, b.S));
+    sl.push_back(reduce(s, RED_DOT, nn, b.X, b.dS));
+    sl.push_back(reduce(s, RED_DOT, nn, b.dX, b.S));
+    sl.push_back(reduce(s, RED_DOT, nn, b.dX, b.dS));
+  }
+  int lin = -1;
+  if (s->ns) {
+    LAUNCH(s, k_aff_lin, s->ns, s->ns, a, bt, s->x, s->dx, s->z, s->dz, s->vlin);
+    lin = reduce(s, RED_SUM, s->ns, s->vlin);
+  }
+  if (!fetch(s)) return false;
+  double v = 0.0;
+  for (size_t i = 0; i < sl.size(); i += 4) {
+    v += s->hslots[sl[i]];
+    v += bt * s->hslots[sl[i + 1]];
+    v += a * s->hslots[sl[i + 2]];
+    v += a * bt * s->hslots[sl[i + 3]];
+  }
+  if (lin >= 0) v += s->hslots[lin];
+  *out = v / std::max(nu(s), 1);
+  return true;
+}
+
+// src/primal_dual.jl:56-72
+bool take_step(S* s, double a, double bt) {
+  s->alpha = a;
+  s->beta = bt;
+  for (auto& b : s->B) {
+    const int64_t nn = (int64_t)b.n * b.n;
+    LAUNCH(s, k_lin, nn, nn, b.X, 1.0, b.X, a, b.dX, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+    LAUNCH(s, k_lin, nn, nn, b.S, 1.0, b.S, bt, b.dS, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+  }
+  if (s->m) LAUNCH(s, k_lin, s->m, s->m, s->y, 1.0, s->y, bt, s->dy, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+  if (s->ns) {
+    LAUNCH(s, k_lin, s->ns, s->ns, s->x, 1.0, s->x, a, s->dx, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+    LAUNCH(s, k_lin, s->ns, s->ns, s->z, 1.0, s->z, bt, s->dz, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+  }
+  s->iter += 1;
+  return update_residuals(s);
+}
+
+bool start_iteration(S* s, bool* ok) {
+  bool p = false, f = false;
+  if (!prepare(s, &p)) return false;
+  if (p && !factorize_schur(s, &f)) return false;
+  *ok = p && f;
+  if (!*ok) s->status = MSDP_ERROR_IN_STEP_COMPUTATION;
+  return true;
+}
+
+// src/primal_dual.jl:85-101
+bool iterate_mehrotra(S* s) {
+  bool ok = false;
+  if (!start_iteration(s, &ok)) return false;
+  if (!ok) return true;
+  double tc = 0.0;
+  if (!total_complementarity(s, &tc)) return false;
+  const double mu = tc / std::max(nu(s), 1);
+  s->mu = mu;
+  solve_directions(s, 0.0, false);
+  double aa = 0, ba = 0, mua = 0;
+  if (!step_lengths(s, &aa, &ba) || !affine_complementarity(s, aa, ba, &mua)) return false;
+  const double sigma = std::min(std::max(std::pow(mua / std::max(mu, kEps), s->comp.sigma_exponent), 1e-8), 1.0);
+  s->sigma = sigma;
+  correction(s);
+  solve_directions(s, sigma * mu, true);
+  double a = 0, bt = 0;
+  if (!step_lengths(s, &a, &bt)) return false;
+  return take_step(s, a, bt);
+}
+
+// src/primal_dual.jl:104-121
+bool iterate_adaptive(S* s) {
+  bool ok = false;
+  if (!start_iteration(s, &ok)) return false;
+  if (!ok) return true;
+  solve_directions(s, s->mu, false);
+  double a = 0, bt = 0;
+  if (!step_lengths(s, &a, &bt) || !take_step(s, a, bt)) return false;
+  double tc = 0.0;
+  if (!total_complementarity(s, &tc)) return false;
+  double mu = s->comp.ratio * tc / std::max(nu(s), 1);
+  if (std::min(a, bt) < 0.5) mu *= 1.5;
+  if (a + bt > 1.6) mu *= 0.75;
+  if (a + bt > 1.9) mu /= 1.0 + 0.1 * s->iter;
+  s->mu = mu;
+  return true;
+}
+
+// S_i = sym(C_i - A_i*(y)), z = d_lin - C_lin'y (src/solver.jl:192-211)
+void set_dual_slacks(S* s) {
+  for (auto& b : s->B) {
+    const int64_t nn = (int64_t)b.n * b.n;
+    jtprod(s, b, s->y, b.T1);
+    LAUNCH(s, k_lin, nn, nn, b.S, 1.0, b.C, -1.0, b.T1, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+    LAUNCH(s, k_sym, nn, b.n, b.S);
+  }
+  if (s->ns) {
+    const double one = 1.0, zero = 0.0;
+    if (s->m) CB(s, cublasDgemv(s->cb, CUBLAS_OP_T, s->m, s->ns, &one, s->Clin, s->m, s->y, 1, &zero, s->ctv, 1));
+    else CU(s, cudaMemsetAsync(s->ctv, 0, sizeof(double) * s->ns, s->st));
+    LAUNCH(s, k_lin, s->ns, s->ns, s->z, 1.0, s->dlin, -1.0, s->ctv, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+  }
+}
+
+// Initial points (src/solver.jl:213-284); returns MSDP_ERR_INITIAL_POINT
+// when DualShift finds no interior point.
+int initial_point(S* s) {
+  const int ip = s->comp.initial_point;
+  if (ip == MSDP_SCALED_IDENTITY) {
+    double beta;
+    if (s->comp.scale > 0.0) {
+      beta = s->comp.scale;
+    } else {
+      double cs = s->cmax;
+      if (s->ns) cs = std::max(cs, s->dnorm);
+      beta = std::max(10.0, std::sqrt(std::max(s->bnorm, 1.0) * std::max(cs, 1.0)) * std::sqrt((double)nu(s)));
+    }
+    for (auto& b : s->B) {
+      LAUNCH(s, k_identity, (int64_t)b.n * b.n, b.n, b.X, beta);
+      LAUNCH(s, k_identity, (int64_t)b.n * b.n, b.n, b.S, beta);
+    }
+    if (s->m) CU(s, cudaMemsetAsync(s->y, 0, sizeof(double) * s->m, s->st));
+    if (s->ns) {
+      LAUNCH(s, k_fill, s->ns, s->ns, s->x, beta);
+      LAUNCH(s, k_fill, s->ns, s->ns, s->z, beta);
+    }
+    return MSDP_OK;
+  }
+  if (ip == MSDP_INITIAL_POINT) {
+    if (!s->has_ip) return MSDP_ERR_INVALID_ARGUMENT;
+    if (s->m) CU(s, cudaMemcpyAsync(s->y, s->ipy.data(), 8 * s->m, cudaMemcpyHostToDevice, s->st));
+    for (int i = 0; i < s->nb; ++i)
+      CU(s, cudaMemcpyAsync(s->B[i].X, s->ipX[i].data(), 8 * s->ipX[i].size(), cudaMemcpyHostToDevice, s->st));
+    if (s->ns) CU(s, cudaMemcpyAsync(s->x, s->ipx.data(), 8 * s->ns, cudaMemcpyHostToDevice, s->st));
+    set_dual_slacks(s);
+    CU(s, cudaStreamSynchronize(s->st));
+    return MSDP_OK;
+  }
+  // DualShift
+  for (auto& b : s->B) LAUNCH(s, k_identity, (int64_t)b.n * b.n, b.n, b.X, 1.0);
+  if (s->ns) LAUNCH(s, k_fill, s->ns, s->ns, s->x, 1.0);
+  double rho = 0.0;
+  while (rho <= s->comp.max_shift) {
+    if (s->m) LAUNCH(s, k_fill, s->m, s->m, s->y, -rho);
+    set_dual_slacks(s);
+    reset_slots(s);
+    std::vector<CholCheck> cc;
+    for (auto& b : s->B) cc.push_back(chol_factor(s, b.n, b.S, b.Ls));
+    const int zmin = s->ns ? reduce(s, RED_MIN, s->ns, s->z) : -1;
+    if (!fetch(s)) return s->fail;
+    bool interior = true;
+    for (auto& c : cc) interior = interior && chol_ok(s, c);
+    if (s->ns) interior = interior && s->hslots[zmin] > 0.0;
+    if (interior) {
+      if (rho != 0.0) {
+        if (s->m) LAUNCH(s, k_fill, s->m, s->m, s->y, -2.0 * rho);
+        set_dual_slacks(s);
+      }
+      return MSDP_OK;
+    }
+    rho = rho == 0.0 ? s->comp.initial_shift : 2.0 * rho;
+  }
+  return MSDP_ERR_INITIAL_POINT;
+}
+
+int initialize(S* s) {
+  const int rc = initial_point(s);
+  if (rc) return rc;
+  s->iter = 0;
+  s->status = MSDP_REGULAR;
+  s->alpha = s->beta = s->sigma = 0.0;
+  s->traj.clear();
+  s->t0 = now_s();
+  if (!update_residuals(s)) return MSDP_ERR_CUDA;
+  double tc = 0.0;
+  if (!total_complementarity(s, &tc)) return MSDP_ERR_CUDA;
+  const double mu = tc / std::max(nu(s), 1);
+  s->mu = s->comp.centering == MSDP_ADAPTIVE_MU ? s->comp.initial_ratio * mu : mu;
+  return MSDP_OK;
+}
+
+void release(S* s) {
+  if (s->st) cudaStreamSynchronize(s->st);
+  for (void* p : s->allocs) cudaFree(p);
+  s->allocs.clear();
+  if (s->hslots) cudaFreeHost(s->hslots);
+  if (s->hinfo) cudaFreeHost(s->hinfo);
+  if (s->cb) cublasDestroy(s->cb);
+  if (s->cs) cusolverDnDestroy(s->cs);
+}
+
+}  // namespace
+
+extern "C" {
+
+int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp_components* comp,
+                       const msdp_options* opt, msdp_solver** out) {
+  if (!ctx || !d || !out) return MSDP_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  msdp_components c;
+  msdp_options o;
+  if (comp) c = *comp; else msdp_default_components(&c);
+  if (opt) o = *opt; else msdp_default_options(&o);
+  if (d->nblocks < 0 || d->m < 0 || d->ns < 0 || (d->nblocks == 0 && d->ns == 0)) return MSDP_ERR_INVALID_ARGUMENT;
+  if (c.algorithm != MSDP_PRIMAL_DUAL || c.schur != MSDP_DENSE_CHOLESKY || c.precision != MSDP_FP64)
+    return MSDP_ERR_UNSUPPORTED;
+  if (!(c.tau > 0.0) || !(c.shrink > 0.0 && c.shrink < 1.0) || !(c.boundary > 0.0 && c.boundary <= 1.0) ||
+      o.max_iter < 0 || (c.initial_point == MSDP_DUAL_SHIFT && !(c.initial_shift > 0.0)))
+    return MSDP_ERR_INVALID_ARGUMENT;
+  auto s = new msdp_solver();
+  s->ctx = ctx;
+  s->st = (cudaStream_t)msdp_context_stream(ctx);
+  s->comp = c;
+  s->opt = o;
+  s->m = d->m;
+  s->ns = d->ns;
+  s->nb = d->nblocks;
+  const int m = d->m, ns = d->ns;
+  int rc = MSDP_OK;
+  auto bail = [&](int code) {
+    release(s);
+    delete s;
+    return code;
+  };
+  if (cublasCreate(&s->cb) != CUBLAS_STATUS_SUCCESS || cusolverDnCreate(&s->cs) != CUSOLVER_STATUS_SUCCESS)
+    return bail(MSDP_ERR_CUDA);
+  cublasSetStream(s->cb, s->st);
+  cusolverDnSetStream(s->cs, s->st);
+  // ---- host staging of the constraints
+  s->B.resize(s->nb);
+  double cmax = 0.0;
+  int64_t dense_ws = 0;
+  for (int i = 0; i < s->nb; ++i) {
+    Blk& b = s->B[i];
+    b.n = d->sides[i];
+    b.nnz = d->A_nnz[i];
+    if (b.n <= 0 || b.nnz < 0) return bail(MSDP_ERR_INVALID_ARGUMENT);
+    const double n = b.n;
+    const double pair_cost = (double)b.nnz * (double)b.nnz;
+    const double dense_cost = 4.0 * n * n * n * m + 2.0 * (double)m * m * n * n;
+    b.dense = m > 0 && pair_cost > dense_cost && n * n * m * 8.0 * 3.0 < 96e9;
+    if (b.dense) dense_ws = std::max<int64_t>(dense_ws, (int64_t)b.n * b.n * m);
+  }
+  // ---- device allocations
+  auto vec = [&](int64_t k) { return dalloc<double>(s, k); };
+  s->b = vec(m); s->dlin = vec(ns); s->Clin = vec((int64_t)m * ns); s->Cw = vec((int64_t)m * ns);
+  s->y = vec(m); s->dy = vec(m); s->Rp = vec(m); s->h = vec(m); s->acc = vec(m);
+  s->x = vec(ns); s->z = vec(ns); s->dx = vec(ns); s->dz = vec(ns); s->Rdlin = vec(ns); s->zinv = vec(ns);
+  s->corrlin = vec(ns); s->vlin = vec(ns); s->ctv = vec(ns); s->wlin = vec(ns);
+  s->H = vec((int64_t)m * m); s->H0 = vec((int64_t)m * m);
+  if (dense_ws) { s->Tb = vec(dense_ws); s->Bb = vec(dense_ws); }
+  s->partial = vec(kRedBlocks); s->slots = vec(kSlots);
+  s->dinfo = dalloc<int>(s, kInfos);
+  bool okalloc = s->b && s->dlin && s->Clin && s->Cw && s->y && s->dy && s->Rp && s->h && s->acc && s->x && s->z &&
+                 s->dx && s->dz && s->Rdlin && s->zinv && s->corrlin && s->vlin && s->ctv && s->wlin && s->H &&
+                 s->H0 && s->partial && s->slots && s->dinfo && (!dense_ws || (s->Tb && s->Bb));
+  if (!okalloc) return bail(MSDP_ERR_OUT_OF_MEMORY);
+  if (cudaMallocHost((void**)&s->hslots, sizeof(double) * kSlots) != cudaSuccess ||
+      cudaMallocHost((void**)&s->hinfo, sizeof(int) * kInfos) != cudaSuccess)
+    return bail(MSDP_ERR_OUT_OF_MEMORY);
+  int lwork = 0;
+  for (int i = 0; i < s->nb; ++i) {
+    Blk& b = s->B[i];
+    const int n = b.n;
+    const int64_t nn = (int64_t)n * n;
+    double** mats[] = {&b.C, &b.X, &b.S, &b.Rd, &b.Ls, &b.Si, &b.Lx, &b.W, &b.G, &b.Gi,
+                       &b.dX, &b.dS, &b.corr, &b.ERd, &b.T1, &b.T2, &b.T3};
+    for (double** p : mats) {
+      *p = vec(nn);
+      if (!*p) return bail(MSDP_ERR_OUT_OF_MEMORY);
+    }
+    b.lam = vec(n); b.D = vec(n); b.sc = vec(n); b.w = vec(n);
+    if (!b.lam || !b.D || !b.sc || !b.w) return bail(MSDP_ERR_OUT_OF_MEMORY);
+    int lw = 0;
+    cusolverDnDpotrf_bufferSize(s->cs, CUBLAS_FILL_MODE_LOWER, n, b.X, n, &lw); lwork = std::max(lwork, lw);
+    cusolverDnDpotri_bufferSize(s->cs, CUBLAS_FILL_MODE_LOWER, n, b.X, n, &lw); lwork = std::max(lwork, lw);
+    cusolverDnDsyevd_bufferSize(s->cs, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, b.X, n, b.lam, &lw);
+    lwork = std::max(lwork, lw);
+    // constraints
+    const int32_t *con = d->A_con[i], *row = d->A_row[i], *col = d->A_col[i];
+    const double* val = d->A_val[i];
+    for (int64_t e = 0; e < b.nnz; ++e)
+      if (con[e] < 0 || con[e] >= m || row[e] < 0 || row[e] >= n || col[e] < 0 || col[e] >= n)
+        return bail(MSDP_ERR_INVALID_ARGUMENT);
+    double cn = 0.0;
+    for (int64_t k = 0; k < nn; ++k) cn = std::max(cn, std::fabs(d->C[i][k]));
+    b.cnorm = cn;
+    cmax = std::max(cmax, cn);
+    CU(s, cudaMemcpy(b.C, d->C[i], 8 * nn, cudaMemcpyHostToDevice));
+    if (b.dense) {
+      std::vector<double> Ad((size_t)nn * m, 0.0);
+      for (int64_t e = 0; e < b.nnz; ++e) Ad[(size_t)con[e] * nn + row[e] + (int64_t)col[e] * n] += val[e];
+      b.Aall = vec(nn * m);
+      if (!b.Aall) return bail(MSDP_ERR_OUT_OF_MEMORY);
+      CU(s, cudaMemcpy(b.Aall, Ad.data(), 8 * Ad.size(), cudaMemcpyHostToDevice));
+    } else {
+      const int64_t nnz = b.nnz;
+      std::vector<int64_t> idx(nnz);
+      std::iota(idx.begin(), idx.end(), 0);
+      std::stable_sort(idx.begin(), idx.end(), [&](int64_t a1, int64_t a2) {
+        if (con[a1] != con[a2]) return con[a1] < con[a2];
+        if (col[a1] != col[a2]) return col[a1] < col[a2];
+        return row[a1] < row[a2];
+      });
+      std::vector<int64_t> cptr(m + 1, 0), pptr(nn + 1, 0);
+      std::vector<int32_t> er(nnz), ec(nnz), pc(nnz);
+      std::vector<double> ev(nnz), pv(nnz);
+      for (int64_t e = 0; e < nnz; ++e) {
+        const int64_t q = idx[e];
+        er[e] = row[q]; ec[e] = col[q]; ev[e] = val[q];
+        cptr[con[q] + 1] += 1;
+        pptr[row[q] + (int64_t)col[q] * n + 1] += 1;
+      }
+      for (int j = 0; j < m; ++j) cptr[j + 1] += cptr[j];
+      for (int64_t k = 0; k < nn; ++k) pptr[k + 1] += pptr[k];
+      std::vector<int64_t> fill(pptr.begin(), pptr.end() - 1);
+      for (int64_t e = 0; e < nnz; ++e) {
+        const int64_t q = idx[e];
+        const int64_t p = fill[row[q] + (int64_t)col[q] * n]++;
+        pc[p] = con[q]; pv[p] = val[q];
+      }
+      b.conptr = dalloc<int64_t>(s, m + 1); b.posptr = dalloc<int64_t>(s, nn + 1);
+      b.erow = dalloc<int32_t>(s, nnz); b.ecol = dalloc<int32_t>(s, nnz); b.pcon = dalloc<int32_t>(s, nnz);
+      b.eval = vec(nnz); b.pval = vec(nnz);
+      if (!b.conptr || !b.posptr || !b.erow || !b.ecol || !b.pcon || !b.eval || !b.pval)
+        return bail(MSDP_ERR_OUT_OF_MEMORY);
+      CU(s, cudaMemcpy(b.conptr, cptr.data(), 8 * (m + 1), cudaMemcpyHostToDevice));
+      CU(s, cudaMemcpy(b.posptr, pptr.data(), 8 * (nn + 1), cudaMemcpyHostToDevice));
+      if (nnz) {
+        CU(s, cudaMemcpy(b.erow, er.data(), 4 * nnz, cudaMemcpyHostToDevice));
+        CU(s, cudaMemcpy(b.ecol, ec.data(), 4 * nnz, cudaMemcpyHostToDevice));
+        CU(s, cudaMemcpy(b.pcon, pc.data(), 4 * nnz, cudaMemcpyHostToDevice));
+        CU(s, cudaMemcpy(b.eval, ev.data(), 8 * nnz, cudaMemcpyHostToDevice));
+        CU(s, cudaMemcpy(b.pval, pv.data(), 8 * nnz, cudaMemcpyHostToDevice));
+      }
+    }
+  }
+  if (m) {
+    int lw = 0;
+    cusolverDnDpotrf_bufferSize(s->cs, CUBLAS_FILL_MODE_LOWER, m, s->H, m, &lw);
+    lwork = std::max(lwork, lw);
+  }
+  s->lwork = std::max(lwork, 1);
+  s->work = vec(s->lwork);
+  if (!s->work) return bail(MSDP_ERR_OUT_OF_MEMORY);
+  double bn = 0.0, dn = 0.0;
+  for (int j = 0; j < m; ++j) bn = std::max(bn, std::fabs(d->b[j]));
+  for (int k = 0; k < ns; ++k) dn = std::max(dn, std::fabs(d->d_lin[k]));
+  s->bnorm = bn; s->dnorm = dn; s->cmax = cmax;
+  if (m) CU(s, cudaMemcpy(s->b, d->b, 8 * m, cudaMemcpyHostToDevice));
+  if (ns) CU(s, cudaMemcpy(s->dlin, d->d_lin, 8 * ns, cudaMemcpyHostToDevice));
+  if (ns && m) CU(s, cudaMemcpy(s->Clin, d->C_lin, 8 * (int64_t)m * ns, cudaMemcpyHostToDevice));
+  if (s->fail) return bail(s->fail);
+  (void)rc;
+  *out = s;
+  return MSDP_OK;
+}
+
+int msdp_solver_destroy(msdp_solver* s) {
+  if (!s) return MSDP_OK;
+  release(s);
+  delete s;
+  return MSDP_OK;
+}
+
+int msdp_solver_set_initial_point(msdp_solver* s, const double* const* X, const double* y, const double* x) {
+  if (!s || (s->m && !y) || (s->nb && !X)) return MSDP_ERR_INVALID_ARGUMENT;
+  s->ipX.assign(s->nb, {});
+  for (int i = 0; i < s->nb; ++i) {
+    const int64_t nn = (int64_t)s->B[i].n * s->B[i].n;
+    if (!X[i]) return MSDP_ERR_INVALID_ARGUMENT;
+    s->ipX[i].assign(X[i], X[i] + nn);
+  }
+  s->ipy.assign(y, y + s->m);
+  if (x) s->ipx.assign(x, x + s->ns); else s->ipx.assign(s->ns, 1.0);
+  s->has_ip = true;
+  return MSDP_OK;
+}
+
+int msdp_solver_solve(msdp_solver* s) {
+  if (!s) return MSDP_ERR_INVALID_ARGUMENT;
+  s->fail = 0;
+  const double t0 = now_s();
+  int rc = initialize(s);
+  if (rc) return rc;
+  if (!update_termination(s)) return s->fail ? s->fail : MSDP_ERR_CUDA;
+  while (s->status == MSDP_REGULAR) {
+    const bool ok = s->comp.centering == MSDP_ADAPTIVE_MU ? iterate_adaptive(s) : iterate_mehrotra(s);
+    if (!ok) return s->fail ? s->fail : MSDP_ERR_CUDA;
+    if (s->status != MSDP_REGULAR) break;
+    if (!update_termination(s)) return s->fail ? s->fail : MSDP_ERR_CUDA;
+  }
+  s->solve_s = now_s() - t0;
+  return MSDP_OK;
+}
+
+int msdp_solver_get_stats(const msdp_solver* s, msdp_stats* o) {
+  if (!s || !o) return MSDP_ERR_INVALID_ARGUMENT;
+  std::memset(o, 0, sizeof(*o));
+  o->status = s->status; o->iter = s->iter; o->iter_fp64 = s->iter; o->iter_fp32 = 0;
+  o->pobj = s->pobj; o->dobj = s->dobj; o->inf_pr = s->inf_pr; o->inf_du = s->inf_du; o->gap = s->gap;
+  o->mu = s->mu; o->sigma = s->sigma; o->alpha = s->alpha; o->beta = s->beta; o->solve_ns = s->solve_s * 1e9;
+  return MSDP_OK;
+}
+
+int msdp_solver_get_solution(msdp_solver* s, double* const* X, double* y, double* x, double* z) {
+  if (!s) return MSDP_ERR_INVALID_ARGUMENT;
+  s->fail = 0;
+  for (int i = 0; X && i < s->nb; ++i)
+    if (X[i]) CU(s, cudaMemcpyAsync(X[i], s->B[i].X, 8 * (int64_t)s->B[i].n * s->B[i].n, cudaMemcpyDeviceToHost, s->st));
+  if (y && s->m) CU(s, cudaMemcpyAsync(y, s->y, 8 * s->m, cudaMemcpyDeviceToHost, s->st));
+  if (x && s->ns) CU(s, cudaMemcpyAsync(x, s->x, 8 * s->ns, cudaMemcpyDeviceToHost, s->st));
+  if (z && s->ns) CU(s, cudaMemcpyAsync(z, s->z, 8 * s->ns, cudaMemcpyDeviceToHost, s->st));
+  CU(s, cudaStreamSynchronize(s->st));
+  return s->fail;
+}
+
+int msdp_solver_get_trajectory(const msdp_solver* s, msdp_iter_record* out, int32_t capacity, int32_t* count) {
+  if (!s || !count) return MSDP_ERR_INVALID_ARGUMENT;
+  *count = (int32_t)s->traj.size();
+  for (int32_t k = 0; out && k < capacity && k < *count; ++k) out[k] = s->traj[k];
+  return MSDP_OK;
+}
+
+int64_t msdp_solver_device_bytes(const msdp_solver* s) { return s ? s->bytes : 0; }
+int64_t msdp_solver_launch_count(const msdp_solver* s) { return s ? s->launches : 0; }
+const char* msdp_solver_last_error(const msdp_solver* s) { return s ? s->err.c_str() : "no solver"; }
+
+}  // extern "C"

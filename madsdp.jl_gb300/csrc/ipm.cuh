@@ -587,6 +587,34 @@ struct Algo {
   __noinline__ __device__ void schur_block_add(const Blk<T>& b, const T* Lg, const T* Rg, T* H) {
     const int n = b.n, m = P.m;
     const int64_t nn = b.nn;
+    if (b.structure == STRUCT_DENSE) {
+      // by columns: T_k = L A_k R, then H_jk = <A_j, T_k> = A_j(T_k) for j >= k
+      T* Ak = b.W(W_T1);
+      T* Lk = b.W(W_T2);
+      T* Tk = b.W(W_T3);
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      for (int k = 0; k < m; ++k) {
+        for (int64_t q = threadIdx.x; q < nn; q += NTHREADS) Ak[q] = (T)0;
+        __syncthreads();
+        for (int64_t q = b.cptr[k] + threadIdx.x; q < b.cptr[k + 1]; q += NTHREADS)
+          atomicAdd(&Ak[b.erow[q] + (int64_t)b.ecol[q] * n], (T)b.eval[q]);
+        __syncthreads();
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, Lg, Ak, (T)0, Lk, scr());
+        cta_gemm<T>(n, 0, 0, 0, 0, (T)1, Lk, Rg, (T)0, Tk, scr());
+        for (int j = k + warp; j < m; j += NWARPS) {
+          T acc = (T)0;
+          for (int64_t q = b.cptr[j] + lane; q < b.cptr[j + 1]; q += 32)
+            acc = fma((T)b.eval[q], Tk[b.erow[q] + (int64_t)b.ecol[q] * n], acc);
+          acc = warp_sum(acc);
+          if (lane == 0) {
+            H[j + (int64_t)k * m] += acc;
+            if (j != k) H[k + (int64_t)j * m] += acc;
+          }
+        }
+        __syncthreads();
+      }
+      return;
+    }
     const T* L = Lg;
     const T* R = Rg;
     const int64_t need = (Lg == Rg ? 1 : 2) * nn * (int64_t)sizeof(T);

@@ -295,6 +295,13 @@ __global__ void msdp_gather_scalars(const __grid_constant__ BatchDev B, double* 
   Prob P = make_prob(B, p);
   for (int k = threadIdx.x; k < SC_COUNT; k += blockDim.x) out[(int64_t)p * SC_COUNT + k] = P.sc[k];
 }
+
+// Copy the scalar blocks of the listed problems into out[count * SC_COUNT].
+__global__ void msdp_gather_scalars_idx(const __grid_constant__ BatchDev B, const int32_t* idx, double* out) {
+  const int q = blockIdx.x;
+  Prob P = make_prob(B, idx[q]);
+  for (int k = threadIdx.x; k < SC_COUNT; k += blockDim.x) out[(int64_t)q * SC_COUNT + k] = P.sc[k];
+}
 #endif
 
 }  // namespace

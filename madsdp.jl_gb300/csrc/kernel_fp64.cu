@@ -21,3 +21,9 @@ cudaError_t msdp_gather_launch(const BatchDev& B, double* out, cudaStream_t stre
   msdp_gather_scalars<<<B.nprob, 64, 0, stream>>>(B, out);
   return cudaGetLastError();
 }
+
+cudaError_t msdp_gather_launch_idx(const BatchDev& B, const int32_t* idx, int count, double* out, cudaStream_t stream) {
+  if (count <= 0) return cudaSuccess;
+  msdp_gather_scalars_idx<<<count, 64, 0, stream>>>(B, idx, out);
+  return cudaGetLastError();
+}

@@ -15,6 +15,7 @@
 
 
 cudaError_t msdp_gather_launch(const BatchDev& B, double* out, cudaStream_t stream);
+cudaError_t msdp_gather_launch_idx(const BatchDev& B, const int32_t* idx, int count, double* out, cudaStream_t stream);
 
 cudaError_t msdp_ipm_setup_0();
 cudaError_t msdp_ipm_setup_1();

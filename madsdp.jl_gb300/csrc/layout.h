@@ -60,7 +60,17 @@ struct ProbDesc {
 };
 
 // constraint structure of a block (detected at upload)
-enum { STRUCT_GENERAL = 0, STRUCT_HANKEL = 1 };
+enum { STRUCT_GENERAL = 0, STRUCT_HANKEL = 1, STRUCT_DENSE = 2 };
+
+// Schur assembly of one block: Hankel 0/1 constraints by their closed form;
+// otherwise entry pairs (cost nnz^2) unless forming T_k = L A_k R per
+// constraint and reading A_j(T_k) (cost m (4 n^3 + nnz)) is cheaper.
+__host__ __device__ inline int choose_structure(bool hankel, int64_t n, int64_t m, int64_t nnz) {
+  if (hankel) return STRUCT_HANKEL;
+  const double pairs = (double)nnz * (double)nnz;
+  const double cols = (double)m * (4.0 * (double)n * (double)n * (double)n + (double)nnz);
+  return pairs > 2.0 * cols ? STRUCT_DENSE : STRUCT_GENERAL;
+}
 
 struct BlockDesc {
   int32_t n, structure;

@@ -52,7 +52,7 @@ __global__ void static_prepare_kernel(BatchDev B, const int32_t* raw_con, const 
       double cn = 0.0;
       for (int64_t k = 0; k < nn; ++k) cn = fmax(cn, fabs(C[k]));
       bd.cnorm = cn;
-      bd.structure = STRUCT_GENERAL;
+      bd.structure = choose_structure(false, n, m, nnz);
       cmax = fmax(cmax, cn);
       const int32_t* con = raw_con + bd.ent;
       const int32_t* row = raw_row + bd.ent;

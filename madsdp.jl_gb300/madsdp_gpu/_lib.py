@@ -92,8 +92,26 @@ SIGNATURES = [
     ("msdp_batch_launch_count", i64, [C.c_void_p]),
     ("msdp_batch_get_profile", i32, [C.c_void_p, i32, P(f64), i32]),
     ("msdp_profile_field_name", C.c_char_p, [i32]),
+    ("msdp_server_create", i32, [C.c_void_p, P(Components), P(Options), i64, i32, P(C.c_void_p)]),
+    ("msdp_server_destroy", i32, [C.c_void_p]),
+    ("msdp_server_submit", i32, [C.c_void_p, P(ProblemDesc), P(i64)]),
+    ("msdp_server_step", i32, [C.c_void_p, i32, P(i32), P(i32)]),
+    ("msdp_server_counts", i32, [C.c_void_p, P(i32), P(i32), P(i64)]),
+    ("msdp_server_result", i32, [C.c_void_p, i64, P(Stats), P(P(f64)), P(f64), P(f64), P(f64), P(f64)]),
+    ("msdp_server_finished", i32, [C.c_void_p, P(i64), i32, P(i32)]),
+    ("msdp_server_launch_count", i64, [C.c_void_p]),
     ("msdp_solve_static", i32, [P(ProblemDesc), P(Components), P(Options), C.c_void_p, P(P(f64)), P(f64),
                                 P(f64), P(f64), P(Stats)]),
+    ("msdp_solver_create", i32, [C.c_void_p, P(ProblemDesc), P(Components), P(Options), P(C.c_void_p)]),
+    ("msdp_solver_destroy", i32, [C.c_void_p]),
+    ("msdp_solver_set_initial_point", i32, [C.c_void_p, P(P(f64)), P(f64), P(f64)]),
+    ("msdp_solver_solve", i32, [C.c_void_p]),
+    ("msdp_solver_get_stats", i32, [C.c_void_p, P(Stats)]),
+    ("msdp_solver_get_solution", i32, [C.c_void_p, P(P(f64)), P(f64), P(f64), P(f64)]),
+    ("msdp_solver_get_trajectory", i32, [C.c_void_p, P(IterRecord), i32, P(i32)]),
+    ("msdp_solver_device_bytes", i64, [C.c_void_p]),
+    ("msdp_solver_launch_count", i64, [C.c_void_p]),
+    ("msdp_solver_last_error", C.c_char_p, [C.c_void_p]),
 ]
 
 _lib = None

@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import weakref
 from typing import List, Optional, Sequence
 
 import numpy as np
@@ -46,6 +47,11 @@ class Context:
             raise GPUError(f"msdp_context_create failed ({_lib.ERRORS.get(rc, rc)})")
         self.h = h
         self.device = device
+        self._children = weakref.WeakSet()
+
+    def adopt(self, child):
+        """Register a batch or server so that closing the context closes it first."""
+        self._children.add(child)
 
     @property
     def stream_handle(self) -> int:
@@ -69,6 +75,8 @@ class Context:
 
     def close(self):
         if getattr(self, "h", None):
+            for child in list(getattr(self, "_children", ())):
+                child.close()
             self.lib.msdp_context_destroy(self.h)
             self.h = None
 
@@ -201,6 +209,7 @@ class Batch:
         rc = self.lib.msdp_batch_create(self.ctx.h, descs, len(marsh), C.byref(comp), C.byref(opts), C.byref(h))
         self.ctx.check(rc, "msdp_batch_create")
         self.h = h
+        self.ctx.adopt(self)
         self.nprob = len(marsh)
         if isinstance(self.initial_point, InitialPoint):
             for p in range(self.nprob):
@@ -370,34 +379,147 @@ def _stats_dict(s) -> dict:
     return d
 
 
-class MadSDPSolver:
-    """One problem on the GPU with the constructor of src/solver.jl:87-160."""
+class InstanceSolver:
+    """One large problem on the whole GPU (msdp_solver): each iteration runs
+    as device-wide operations instead of one thread block per problem."""
 
-    def __init__(self, model: Model, **kwargs):
+    def __init__(self, model: Model, algorithm=None, direction=None, step=None, centering=None,
+                 initial_point=None, schur=None, precision: str = "fp64", context: Optional[Context] = None,
+                 **options):
+        self.ctx = context or default_context()
+        self.lib = self.ctx.lib
         self.model = model
-        self.batch = Batch([model], **kwargs)
+        direction = NT() if direction is None else direction
+        step = EigenStep() if step is None else step
+        centering = Mehrotra() if centering is None else centering
+        self.algorithm = PrimalDual(direction, step, centering) if algorithm is None else algorithm
+        self.initial_point = ScaledIdentity() if initial_point is None else initial_point
+        self.schur = DenseCholesky() if schur is None else schur
+        self.opt = Options(**options)
+        mm = _Marshalled(model)
+        comp = _components(self.algorithm, self.initial_point, self.schur, precision)
+        opts = _options(self.opt)
+        h = C.c_void_p()
+        rc = self.lib.msdp_solver_create(self.ctx.h, C.byref(mm.desc), C.byref(comp), C.byref(opts), C.byref(h))
+        if rc == -4:
+            raise NotImplementedError("the whole-GPU solver runs PrimalDual with DenseCholesky in FP64")
+        if rc != 0:
+            raise (ValueError if rc == -1 else GPUError)(f"msdp_solver_create: {_lib.ERRORS.get(rc, rc)}")
+        self.h = h
+        self.ctx.adopt(self)
+        if isinstance(self.initial_point, InitialPoint):
+            ip = self.initial_point
+            X = [np.asfortranarray(np.asarray(a, dtype=np.float64)) for a in ip.X]
+            Xp = (f64p * max(len(X), 1))(*[_ptr(a) for a in X])
+            y = np.ascontiguousarray(ip.y, dtype=np.float64)
+            x = None if ip.x is None else np.ascontiguousarray(ip.x, dtype=np.float64)
+            rc = self.lib.msdp_solver_set_initial_point(self.h, Xp, _ptr(y), None if x is None else _ptr(x))
+            if rc != 0:
+                raise ValueError("msdp_solver_set_initial_point: invalid initial point")
+        self._stats = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.msdp_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self):
+        rc = self.lib.msdp_solver_solve(self.h)
+        if rc == -5:
+            raise RuntimeError("MadSDP: could not find a dual interior point `y = -ρ 1`; use `InitialPoint` to give one.")
+        if rc != 0:
+            msg = self.lib.msdp_solver_last_error(self.h).decode()
+            raise GPUError(f"msdp_solver_solve: {_lib.ERRORS.get(rc, rc)}: {msg}")
+        self._stats = None
+        return self
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.lib.msdp_solver_device_bytes(self.h))
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.msdp_solver_launch_count(self.h))
+
+    def stats(self) -> dict:
+        st = _lib.Stats()
+        self.lib.msdp_solver_get_stats(self.h, C.byref(st))
+        return _stats_dict(st)
+
+    def solution(self):
+        m = self.model
+        X = [np.zeros((n, n), order="F") for n in m.sides]
+        Xp = (f64p * max(len(X), 1))(*[_ptr(a) for a in X])
+        y, x, z = np.zeros(m.m), np.zeros(m.ns), np.zeros(m.ns)
+        rc = self.lib.msdp_solver_get_solution(self.h, Xp, _ptr(y), _ptr(x), _ptr(z))
+        if rc != 0:
+            raise GPUError(f"msdp_solver_get_solution: {_lib.ERRORS.get(rc, rc)}")
+        return [np.ascontiguousarray(a) for a in X], y, x, z
+
+    def trajectory(self) -> List[dict]:
+        cap = self.opt.max_iter + 2
+        arr = (_lib.IterRecord * cap)()
+        cnt = C.c_int32()
+        self.lib.msdp_solver_get_trajectory(self.h, arr, cap, C.byref(cnt))
+        return [{k: getattr(r, k) for k, _ in _lib.IterRecord._fields_} for r in arr[:min(cnt.value, cap)]]
+
+
+def _use_instance_engine(model: Model) -> bool:
+    """Blocks above 160 or more than 600 constraints run on the whole GPU."""
+    return max(model.sides, default=0) > 160 or model.m > 600
+
+
+class MadSDPSolver:
+    """One problem on the GPU with the constructor of src/solver.jl:87-160.
+
+    engine = "batch" runs it as a one-problem batch (one thread block),
+    "instance" on the whole GPU, "auto" picks by size."""
+
+    def __init__(self, model: Model, engine: str = "auto", **kwargs):
+        self.model = model
+        if engine not in ("auto", "batch", "instance"):
+            raise ValueError("engine must be 'auto', 'batch' or 'instance'")
+        if engine == "auto":
+            engine = "instance" if _use_instance_engine(model) else "batch"
+        self.engine = engine
+        self.batch = Batch([model], **kwargs) if engine == "batch" else None
+        self.instance = InstanceSolver(model, **kwargs) if engine == "instance" else None
         self._stats = None
 
     def initialize(self):
+        if self.batch is None:
+            raise NotImplementedError("the whole-GPU engine solves in one call")
         self.batch.initialize()
         self._stats = None
 
     def solve(self, verbose: bool = False):
         """solve!(solver) (src/solver.jl:385-396)."""
-        self.batch.solve()
-        self._stats = self.batch.stats(0)
+        if self.instance is not None:
+            self.instance.solve()
+            self._stats = self.instance.stats()
+        else:
+            self.batch.solve()
+            self._stats = self.batch.stats(0)
         if verbose:
-            print_trajectory(self.batch.trajectory(0))
+            print_trajectory(self.trajectory())
         return self
 
     def iterate(self, k: int = 1):
+        if self.batch is None:
+            raise NotImplementedError("the whole-GPU engine solves in one call")
         self.batch.iterate(k)
         self._stats = None
 
     @property
     def stats(self) -> dict:
         if self._stats is None:
-            self._stats = self.batch.stats(0)
+            self._stats = self.instance.stats() if self.instance is not None else self.batch.stats(0)
         return self._stats
 
     @property
@@ -427,10 +549,10 @@ class MadSDPSolver:
         return self.stats["gap"]
 
     def solution(self):
-        return self.batch.solution(0)
+        return self.instance.solution() if self.instance is not None else self.batch.solution(0)
 
     def trajectory(self):
-        return self.batch.trajectory(0)
+        return self.instance.trajectory() if self.instance is not None else self.batch.trajectory(0)
 
 
 def print_trajectory(traj):

@@ -28,3 +28,14 @@ def build(name: str) -> Model:
 def laplacian(W):
     W = np.asarray(W, dtype=float)
     return np.diag(W.sum(axis=1)) - W
+
+
+def compare_trajectories(gpu_traj, ref_traj, gap_floor=1e-5, rtol=1e-6):
+    """Per iteration, pobj and dobj agree to rtol while the gap is above gap_floor."""
+    n = min(len(gpu_traj), len(ref_traj))
+    for k in range(n):
+        r, q = gpu_traj[k], ref_traj[k]
+        if r["gap"] < gap_floor:
+            break
+        for key in ("pobj", "dobj"):
+            assert abs(q[key] - r[key]) <= rtol * max(1.0, abs(r[key])), (k, key, q[key], r[key])

@@ -1,0 +1,119 @@
+"""Whole-GPU solver of one large problem (msdp_solver) against the oracle:
+known answers, every PrimalDual component, coordinate-list (one-hot,
+Hankel) and dense constraint assembly, scalar blocks, initial points and
+per-iteration trajectories.  Tolerances as in the batch parity tests."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import madsdp_gpu as M
+from madsdp_gpu import generators as g
+from oracle import madsdp_oracle as o
+from problems import build, compare_trajectories
+
+pytestmark = pytest.mark.gpu
+KA = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))
+
+
+def comps(spec, mod):
+    return {k: getattr(mod, v)() for k, v in (spec or {}).items()}
+
+
+def inst(model, **kw):
+    return M.MadSDPSolver(model, engine="instance", **kw).solve()
+
+
+def assert_matches_oracle(s, ref, traj=True, iters=1):
+    assert s.status == M.Status.SOLVE_SUCCEEDED, s.stats
+    assert int(ref.status) == int(M.Status.SOLVE_SUCCEEDED)
+    assert abs(s.iter - ref.iter) <= iters
+    scale = max(1.0, abs(ref.primal_objective()) + abs(ref.dual_objective()))
+    assert abs(s.primal_objective() - ref.primal_objective()) <= 1e-7 * scale
+    assert abs(s.dual_objective() - ref.dual_objective()) <= 1e-7 * scale
+    assert max(s.inf_pr, s.inf_du, s.inf_compl) <= 1e-7
+    if traj:
+        compare_trajectories(s.trajectory(), ref.trajectory)
+
+
+@pytest.mark.parametrize("case", [c for c in KA["cases"] if "objective" in c], ids=lambda c: c["name"])
+def test_known_objective(gpu_ctx, case):
+    s = inst(build(case["model"]), **comps(case.get("components"), M), **case["options"])
+    assert s.engine == "instance"
+    assert abs(s.primal_objective() - case["objective"]) <= case["atol"]
+    ref = o.Solver(build(case["model"]), **comps(case.get("components"), o), **case["options"]).solve()
+    assert_matches_oracle(s, ref, traj=False)
+
+
+@pytest.mark.parametrize("direction", ["NT", "HKM"])
+@pytest.mark.parametrize("step", ["EigenStep", "CholeskyBacktrack"])
+@pytest.mark.parametrize("centering", ["Mehrotra", "AdaptiveMu"])
+def test_component_matrix(gpu_ctx, direction, step, centering):
+    model = g.maxcut(30, 0.2, seed=7)
+    kw = dict(direction=getattr(M, direction)(), step=getattr(M, step)(), centering=getattr(M, centering)())
+    okw = dict(direction=getattr(o, direction)(), step=getattr(o, step)(), centering=getattr(o, centering)())
+    s = inst(model, **kw)
+    ref = o.Solver(model, **okw).solve()
+    assert_matches_oracle(s, ref)
+
+
+def test_maxcut_config1_trajectory(gpu_ctx):
+    """MaxCut n = 100, p = 0.1: one-hot constraints, Schur = W o W."""
+    model = g.maxcut(100, 0.1, seed=0)
+    assert_matches_oracle(inst(model), o.Solver(model).solve())
+
+
+def test_maxcut_pm1_weights_large(gpu_ctx):
+    """MaxCut n = 400 with +-1 weights (the distribution of the n = 2000 case)."""
+    model = g.maxcut(400, 0.02, weights="pm1", seed=3)
+    assert_matches_oracle(inst(model), o.Solver(model).solve())
+
+
+@pytest.mark.parametrize("direction", ["NT", "HKM"])
+def test_dense_mixed_cones(gpu_ctx, direction):
+    """Dense A with two PSD blocks and scalars: the GEMM assembly path."""
+    model = g.dense_random([14, 9], 6, 40, seed=5)
+    s = inst(model, direction=getattr(M, direction)())
+    ref = o.Solver(model, direction=getattr(o, direction)()).solve()
+    assert_matches_oracle(s, ref)
+
+
+def test_sos_hankel_pairs(gpu_ctx):
+    model = g.sos_hankel(40, seed=9)
+    assert_matches_oracle(inst(model), o.Solver(model).solve())
+
+
+def test_mixed_lp_and_solution(gpu_ctx):
+    model = g.mixed_lp_example()
+    s = inst(model)
+    ref = o.Solver(model).solve()
+    assert_matches_oracle(s, ref, traj=False)
+    X, y, x, z = s.solution()
+    np.testing.assert_allclose(X[0], ref.blocks[0].X, atol=1e-6)
+    np.testing.assert_allclose(y, ref.y, atol=1e-6)
+    np.testing.assert_allclose(x, ref.x, atol=1e-6)
+
+
+def test_initial_points(gpu_ctx):
+    model = g.maxcut(40, 0.2, seed=2)
+    L = -4.0 * model.C[0]
+    ip = dict(X=[np.eye(40)], y=-(1.0 + np.abs(L).sum(axis=0)))
+    s = inst(model, initial_point=M.InitialPoint(**ip))
+    ref = o.Solver(model, initial_point=o.InitialPoint(**ip)).solve()
+    assert_matches_oracle(s, ref)
+    s = inst(model, initial_point=M.DualShift())
+    ref = o.Solver(model, initial_point=o.DualShift()).solve()
+    assert_matches_oracle(s, ref)
+    s = inst(model, initial_point=M.ScaledIdentity(50.0))
+    ref = o.Solver(model, initial_point=o.ScaledIdentity(50.0)).solve()
+    assert_matches_oracle(s, ref)
+
+
+def test_auto_engine_and_unsupported(gpu_ctx):
+    assert M.MadSDPSolver(g.maxcut(200, 0.05, seed=1)).engine == "instance"
+    assert M.MadSDPSolver(g.maxcut(30, 0.2, seed=1)).engine == "batch"
+    with pytest.raises(NotImplementedError):
+        M.InstanceSolver(g.maxcut(30, 0.2, seed=1), schur=M.QRSchur())
+    with pytest.raises(NotImplementedError):
+        M.InstanceSolver(g.maxcut(30, 0.2, seed=1), precision="mixed")

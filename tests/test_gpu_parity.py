@@ -12,7 +12,7 @@ import pytest
 import madsdp_gpu as M
 from madsdp_gpu import generators as g
 from oracle import madsdp_oracle as o
-from problems import build, laplacian
+from problems import build, compare_trajectories, laplacian
 
 pytestmark = pytest.mark.gpu
 KA = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))
@@ -140,16 +140,6 @@ def test_newton_identities(gpu_ctx, scalars, diagonal, schur):
         assert np.allclose(W, ref.blocks[0].W, atol=1e-10)
 
 
-def compare_trajectories(gpu_traj, ref_traj, gap_floor=1e-5, rtol=1e-6):
-    n = min(len(gpu_traj), len(ref_traj))
-    for k in range(n):
-        r, q = gpu_traj[k], ref_traj[k]
-        if r["gap"] < gap_floor:
-            break
-        for key in ("pobj", "dobj"):
-            assert abs(q[key] - r[key]) <= rtol * max(1.0, abs(r[key])), (k, key, q[key], r[key])
-
-
 def test_trajectory_maxcut_config1(gpu_ctx):
     """MaxCut n = 100, p = 0.1, NT + EigenStep + Mehrotra + DenseCholesky, FP64."""
     model = g.maxcut(100, 0.1, seed=0)
@@ -214,6 +204,23 @@ def test_batch_uneven_results_independent_of_mix(gpu_ctx):
         assert a["status"] == st_all[i]["status"] == M.Status.SOLVE_SUCCEEDED
         assert a["iter"] == st_all[i]["iter"]
         assert a["pobj"] == st_all[i]["pobj"] and a["dobj"] == st_all[i]["dobj"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("direction", ["NT", "HKM"])
+def test_dense_constraints_column_assembly(gpu_ctx, direction, precision):
+    """Dense A_j (every entry nonzero) takes the column assembly
+    T_k = L A_k R, H_jk = A_j(T_k) instead of entry pairs."""
+    models = [g.dense_random([10], 0, 30, seed=11), g.dense_random([8, 5], 3, 25, seed=12)]
+    bt = M.Batch(models, direction=getattr(M, direction)(), precision=precision)
+    bt.solve()
+    for m, st in zip(models, bt.all_stats()):
+        ref = o.Solver(m, direction=getattr(o, direction)()).solve()
+        assert st["status"] == M.Status.SOLVE_SUCCEEDED, st
+        scale = max(1.0, abs(ref.primal_objective()) + abs(ref.dual_objective()))
+        assert abs(st["pobj"] - ref.primal_objective()) <= (1e-7 if precision == "fp64" else 5e-7) * scale
+        if precision == "fp64":
+            assert abs(st["iter"] - ref.iter) <= 1
 
 
 # ------------------------------------------------------------------ DualCentering

@@ -1,0 +1,120 @@
+"""Continuous-batching server (msdp_server_*): a request's result does not
+depend on what else is on the GPU, on when it was admitted, or on how many
+iterations each wave runs."""
+
+import numpy as np
+import pytest
+
+import madsdp_gpu as M
+from madsdp_gpu import generators as g
+from madsdp_gpu.serving import Server, poisson_stream, serve_stream
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_requests():
+    return [g.sos_hankel(9, seed=11), g.maxcut(24, 0.2, seed=4), g.dense_random([7], 0, 12, seed=3),
+            g.sos_hankel(30, seed=12), g.dense_random([6, 4], 3, 10, seed=2), g.maxcut(40, 0.1, seed=5),
+            g.sos_hankel(5, seed=13), g.dense_random([12], 0, 40, seed=8)]
+
+
+def alone(model, **kw):
+    bt = M.Batch([model], **kw)
+    bt.solve()
+    X, y, x, z = bt.solution(0)
+    return bt.all_stats()[0], X, y
+
+
+def assert_same(r, st, X, y):
+    assert r["status"] == st["status"]
+    assert r["iter"] == st["iter"]
+    scale = max(1.0, abs(st["pobj"]) + abs(st["dobj"]))
+    assert abs(r["pobj"] - st["pobj"]) <= 1e-12 * scale
+    assert abs(r["dobj"] - st["dobj"]) <= 1e-12 * scale
+    for a, b in zip(r["X"], X):
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-10 * max(1.0, np.abs(b).max()))
+    np.testing.assert_allclose(r["y"], y, rtol=0, atol=1e-10 * max(1.0, np.abs(y).max()))
+
+
+def test_server_matches_solving_alone(gpu_ctx):
+    """Requests arrive two per wave while earlier ones are mid-solve."""
+    models = mixed_requests()
+    srv = Server(memory_budget_bytes=64 << 20, max_slots=16)
+    ids = []
+    for k in range(0, len(models), 2):
+        ids += [srv.submit(models[k]), srv.submit(models[k + 1])]
+        srv.step(3)
+    srv.drain(3)
+    assert srv.counts()[2] == len(models)
+    assert sorted(srv.finished()) == sorted(ids) and srv.finished() == []
+    for rid, m in zip(ids, models):
+        r = srv.result(rid)
+        assert r is not None and r["latency_s"] > 0
+        st, X, y = alone(m)
+        assert st["status"] == M.Status.SOLVE_SUCCEEDED
+        assert_same(r, st, X, y)
+    srv.close()
+
+
+@pytest.mark.parametrize("iterations", [1, 7])
+def test_server_wave_length_does_not_change_results(gpu_ctx, iterations):
+    models = mixed_requests()[:4]
+    srv = Server(memory_budget_bytes=32 << 20, max_slots=8)
+    ids = [srv.submit(m) for m in models]
+    srv.drain(iterations)
+    for rid, m in zip(ids, models):
+        st, X, y = alone(m)
+        assert_same(srv.result(rid), st, X, y)
+
+
+def test_server_admits_by_memory(gpu_ctx):
+    """With room for two SOS(63) regions, five requests run at most two at a
+    time, in arrival order, and all finish with the same answers."""
+    models = [g.sos_hankel(63, seed=20 + i) for i in range(5)]
+    srv = Server(memory_budget_bytes=3 << 20, max_slots=8)
+    ids = [srv.submit(m) for m in models]
+    assert srv.result(ids[0]) is None
+    srv.step(2)
+    pending, active, _ = srv.counts()
+    assert 1 <= active <= 2 and pending == 5 - active
+    seen_max = active
+    for _ in range(1000):
+        p, a, _ = srv.counts()
+        if p == 0 and a == 0:
+            break
+        srv.step(2)
+        seen_max = max(seen_max, srv.counts()[1])
+    assert seen_max <= 2
+    for rid, m in zip(ids, models):
+        st, X, y = alone(m)
+        assert_same(srv.result(rid), st, X, y)
+
+
+def test_server_rejects_oversize_and_bad_options(gpu_ctx):
+    srv = Server(memory_budget_bytes=1 << 20, max_slots=2)
+    with pytest.raises(ValueError, match="TOO_LARGE"):
+        srv.submit(g.sos_hankel(63, seed=1))
+    srv.close()
+    with pytest.raises(RuntimeError):
+        Server(memory_budget_bytes=0)
+
+
+def test_server_mixed_precision(gpu_ctx):
+    models = [g.sos_hankel(int(d), seed=40 + i) for i, d in enumerate([6, 18, 33, 47])]
+    srv = Server(memory_budget_bytes=64 << 20, max_slots=8, precision="mixed")
+    ids = [srv.submit(m) for m in models]
+    srv.drain(2)
+    for rid, m in zip(ids, models):
+        r = srv.result(rid)
+        st, X, y = alone(m, precision="mixed")
+        assert r["iter_fp32"] == st["iter_fp32"] and r["iter_fp32"] >= 1
+        assert_same(r, st, X, y)
+
+
+def test_serve_poisson_stream(gpu_ctx):
+    stream = poisson_stream(rate=400.0, duration=0.1, seed=3, sos_d=(5, 20), maxcut_n=(20, 30), dense_n=(6, 10))
+    srv = Server(memory_budget_bytes=256 << 20, max_slots=64)
+    out = serve_stream(srv, stream, iterations=2, time_limit=120.0)
+    assert out["completed"] == out["requests"] == len(stream) > 0
+    assert out["succeeded"] == out["completed"]
+    assert out["p99_latency_ms"] >= out["p50_latency_ms"] > 0
