@@ -216,6 +216,7 @@ def run_instance(args):
     launches = solver.launch_count - launches
     st = solver.stats()
     device_bytes = solver.device_bytes
+    phases = {k: round(v, 4) for k, v in solver.profile().items()}
     solver.close()
     # end to end: upload, solve, download through the public API
     t = time.perf_counter()
@@ -249,7 +250,7 @@ def run_instance(args):
                    "m": model.m, "components": "PrimalDual(NT, EigenStep, Mehrotra) + DenseCholesky, ScaledIdentity",
                    "engine": "whole-GPU instance solver (cuBLAS/cuSOLVER dense algebra + own assembly/residual kernels)",
                    "status": str(st["status"]), "iterations": st["iter"], "pobj": st["pobj"], "gap": st["gap"],
-                   "inf_pr": st["inf_pr"], "inf_du": st["inf_du"],
+                   "inf_pr": st["inf_pr"], "inf_du": st["inf_du"], "phase_seconds_last_solve": phases,
                    "l2": f"{device_bytes / 2**20:.0f} MiB resident"},
         "gpu_launches": launches // max(1, args.steps),
         "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -468,10 +469,12 @@ def run_gpu(args):
                                 sos_d=SERVE_MIX["sos_d"], maxcut_n=SERVE_MIX["maxcut_n"],
                                 dense_n=SERVE_MIX["dense_n"], dense_m=SERVE_MIX["dense_m"])
         srv = Server(memory_budget_bytes=8 << 30, max_slots=4096, precision="mixed", context=ctx)
-        serving = serve_stream(srv, stream, iterations=args.serve_iterations, time_limit=600.0)
+        serving = serve_stream(srv, stream, iterations=args.serve_iterations, time_limit=600.0,
+                               budget_s=args.serve_budget_ms / 1e3)
         srv.close()
         serving.update({"rate_per_s": args.serve_rate, "duration_s": args.serve_seconds,
-                        "iterations_per_wave": args.serve_iterations, "memory_budget_bytes": 8 << 30,
+                        "iterations_per_wave": args.serve_iterations, "wave_budget_ms": args.serve_budget_ms,
+                        "memory_budget_bytes": 8 << 30,
                         "mix": "50%% SOS d~U%s, 30%% max-cut n~U%s p=4/n, 20%% dense one block n~U%s m<=min(%d, n(n+1)/2)"
                                % (SERVE_MIX["sos_d"], SERVE_MIX["maxcut_n"], SERVE_MIX["dense_n"], SERVE_MIX["dense_m"]),
                         "latency": "host clock, arrival to result available"})
@@ -550,7 +553,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=200.0)
-    ap.add_argument("--serve-iterations", type=int, default=2)
+    ap.add_argument("--serve-iterations", type=int, default=1000)
+    ap.add_argument("--serve-budget-ms", type=float, default=20.0)
     ap.add_argument("--workload", default="sos_batch", choices=["sos_batch", *INSTANCE_WORKLOADS])
     args = ap.parse_args()
     if args.workload != "sos_batch":

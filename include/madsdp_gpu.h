@@ -227,6 +227,11 @@ int msdp_server_destroy(msdp_server* server);
 /* Copies the problem; returns MSDP_ERR_TOO_LARGE if it can never fit. */
 int msdp_server_submit(msdp_server* server, const msdp_problem_desc* problem, int64_t* request_id);
 int msdp_server_step(msdp_server* server, int32_t iterations, int32_t* active, int32_t* completed);
+/* Time-sliced wave: every active request runs at least one and at most
+ * `iterations` iterations, stopping once the wave has run `budget_s` seconds,
+ * so small requests finish within one wave while large ones progress. */
+int msdp_server_step_budget(msdp_server* server, int32_t iterations, double budget_s, int32_t* active,
+                            int32_t* completed);
 int msdp_server_counts(const msdp_server* server, int32_t* pending, int32_t* active, int64_t* completed);
 /* 1 while the request is not finished; 0 once its results are copied out
  * (the request is then forgotten).  latency_s = finish - submit, host clock. */
@@ -294,6 +299,11 @@ int msdp_solver_get_stats(const msdp_solver* solver, msdp_stats* out);
 int msdp_solver_get_solution(msdp_solver* solver, double* const* X, double* y, double* x, double* z);
 int msdp_solver_get_trajectory(const msdp_solver* solver, msdp_iter_record* out, int32_t capacity, int32_t* count);
 int64_t msdp_solver_device_bytes(const msdp_solver* solver);
+/* Device seconds per phase of the last solve (prepare, Schur assembly,
+ * Schur factorization, directions, step lengths, correction, take step and
+ * residuals); returns the number of fields written. */
+int msdp_solver_get_profile(const msdp_solver* solver, double* seconds, int32_t capacity);
+const char* msdp_solver_profile_field_name(int32_t index);
 /* Launches of this library's own kernels (library calls not counted). */
 int64_t msdp_solver_launch_count(const msdp_solver* solver);
 const char* msdp_solver_last_error(const msdp_solver* solver);

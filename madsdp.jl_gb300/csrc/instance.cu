@@ -333,6 +333,7 @@ struct msdp_solver {
   double *H = nullptr, *H0 = nullptr, *Tb = nullptr, *Bb = nullptr;
   double* work = nullptr;
   int lwork = 0;
+  double *lq = nullptr, *lh = nullptr;  // Lanczos basis (n x (kLanczosMax + 1)) and projections
   int* dinfo = nullptr;
   double *partial = nullptr, *slots = nullptr;
   double* hslots = nullptr;
@@ -351,11 +352,42 @@ struct msdp_solver {
   int64_t launches = 0;
   int fail = 0;  // first library/CUDA error seen
   std::string err;
+  // per-phase device time: events recorded at phase starts, read after the
+  // synchronization that ends each iteration
+  cudaEvent_t ev[64] = {};
+  int ev_phase[64] = {};
+  int nev = 0;
+  double phase_s[16] = {};
 };
 
 namespace {
 
 using S = msdp_solver;
+
+enum { PH_PREPARE = 0, PH_ASSEMBLY, PH_FACTOR, PH_DIRECTIONS, PH_STEP, PH_CORRECTION, PH_STEP_UPDATE, PH_COUNT };
+const char* kPhaseNames[PH_COUNT] = {"prepare", "schur_assembly", "schur_factor", "directions",
+                                     "step_lengths", "correction", "take_step_residuals"};
+
+void mark(S* s, int phase) {
+  if (s->nev >= 64 || !s->ev[s->nev]) return;
+  cudaEventRecord(s->ev[s->nev], s->st);
+  s->ev_phase[s->nev] = phase;
+  s->nev += 1;
+}
+
+// Close the open phase segments (the stream must be idle).
+void collect_marks(S* s) {
+  if (s->nev == 0) return;
+  if (s->nev < 64 && s->ev[s->nev]) {
+    cudaEventRecord(s->ev[s->nev], s->st);
+    cudaEventSynchronize(s->ev[s->nev]);
+    for (int k = 0; k < s->nev; ++k) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, s->ev[k], s->ev[k + 1]) == cudaSuccess) s->phase_s[s->ev_phase[k]] += 1e-3 * ms;
+    }
+  }
+  s->nev = 0;
+}
 
 #define LAUNCH(s, kern, n, ...)                                          \
   do {                                                                   \
@@ -654,7 +686,9 @@ bool factorize_schur(S* s, bool* ok) {
   const int m = s->m;
   *ok = false;
   if (m == 0) { *ok = true; return true; }
+  mark(s, PH_ASSEMBLY);
   schur_complement(s, s->H0);
+  mark(s, PH_FACTOR);
   double reg = s->opt.regularize_schur;
   for (int t = 0; t < s->opt.max_schur_reg; ++t) {
     reset_slots(s);
@@ -729,6 +763,123 @@ void correction(S* s) {
   if (s->ns) LAUNCH(s, k_corr_lin, s->ns, s->ns, s->dx, s->dz, s->zinv, s->corrlin);
 }
 
+// ---- Lanczos for lambda_min of a formed symmetric Z (blocks above
+// kLanczosMin; smaller blocks use the dense eigensolver).  Full
+// reorthogonalization; stops when the Ritz residual |beta_k s_k| of the
+// smallest Ritz value is below 1e-12 ||Z|| (eigenvalue error at most that),
+// at k = n, or gives up at kLanczosMax (the caller then uses the dense
+// eigensolver).
+constexpr int kLanczosMin = 257;
+constexpr int kLanczosMax = 320;
+
+// number of eigenvalues of the tridiagonal (a, b) below x (Sturm count)
+int sturm_count(const std::vector<double>& a, const std::vector<double>& b, int k, double x) {
+  int c = 0;
+  double d = 1.0;
+  for (int i = 0; i < k; ++i) {
+    d = a[i] - x - (i ? b[i - 1] * b[i - 1] / d : 0.0);
+    if (d == 0.0) d = -1e-300;
+    if (d < 0.0) ++c;
+  }
+  return c;
+}
+
+double tridiag_min(const std::vector<double>& a, const std::vector<double>& b, int k, double* norm) {
+  double lo = INFINITY, hi = -INFINITY;
+  for (int i = 0; i < k; ++i) {
+    const double r = (i > 0 ? std::fabs(b[i - 1]) : 0.0) + (i < k - 1 ? std::fabs(b[i]) : 0.0);
+    lo = std::min(lo, a[i] - r);
+    hi = std::max(hi, a[i] + r);
+  }
+  *norm = std::max(std::fabs(lo), std::fabs(hi));
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    if (sturm_count(a, b, k, mid) >= 1) hi = mid; else lo = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+// |last component| of the unit eigenvector of the tridiagonal for theta
+// (two steps of inverse iteration with a tridiagonal LU)
+double tridiag_last_component(const std::vector<double>& a, const std::vector<double>& b, int k, double theta,
+                              double norm) {
+  const double shift = theta - 1e-14 * std::max(norm, 1e-300);
+  std::vector<double> y(k, 1.0), c(k), d(k);
+  for (int rep = 0; rep < 2; ++rep) {
+    // Thomas algorithm on (T - shift I) y_new = y
+    double piv = a[0] - shift;
+    if (piv == 0.0) piv = 1e-300;
+    c[0] = k > 1 ? b[0] / piv : 0.0;
+    d[0] = y[0] / piv;
+    for (int i = 1; i < k; ++i) {
+      piv = a[i] - shift - b[i - 1] * c[i - 1];
+      if (piv == 0.0) piv = 1e-300;
+      c[i] = i < k - 1 ? b[i] / piv : 0.0;
+      d[i] = (y[i] - b[i - 1] * d[i - 1]) / piv;
+    }
+    y[k - 1] = d[k - 1];
+    for (int i = k - 2; i >= 0; --i) y[i] = d[i] - c[i] * y[i + 1];
+    double nrm = 0.0;
+    for (int i = 0; i < k; ++i) nrm += y[i] * y[i];
+    nrm = std::sqrt(nrm);
+    if (!(nrm > 0.0) || !std::isfinite(nrm)) return 1.0;
+    for (int i = 0; i < k; ++i) y[i] /= nrm;
+  }
+  return std::fabs(y[k - 1]);
+}
+
+bool lanczos_eigmin(S* s, int n, const double* Z, double* out) {
+  double* Q = s->lq;
+  // fixed pseudo-random start vector (xorshift), normalized
+  std::vector<double> q0(n);
+  uint64_t st = 0x9E3779B97F4A7C15ull ^ (uint64_t)n;
+  double nrm = 0.0;
+  for (int i = 0; i < n; ++i) {
+    st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+    q0[i] = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    nrm += q0[i] * q0[i];
+  }
+  nrm = std::sqrt(nrm);
+  for (auto& v : q0) v /= nrm;
+  CU(s, cudaMemcpyAsync(Q, q0.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s->st));
+  std::vector<double> al, be;
+  const double one = 1.0, zero = 0.0, mone = -1.0;
+  double beta_prev = 0.0;
+  const int kmax = std::min(n, kLanczosMax);
+  for (int k = 0; k < kmax; ++k) {
+    const double* q = Q + (int64_t)k * n;
+    double* w = Q + (int64_t)(k + 1) * n;
+    CB(s, cublasDsymv(s->cb, CUBLAS_FILL_MODE_LOWER, n, &one, Z, n, q, 1, &zero, w, 1));
+    double alpha = 0.0;
+    CB(s, cublasDdot(s->cb, n, q, 1, w, 1, &alpha));
+    const double ma = -alpha;
+    CB(s, cublasDaxpy(s->cb, n, &ma, q, 1, w, 1));
+    if (k > 0) {
+      const double mb = -beta_prev;
+      CB(s, cublasDaxpy(s->cb, n, &mb, Q + (int64_t)(k - 1) * n, 1, w, 1));
+    }
+    for (int r = 0; r < 2; ++r) {
+      CB(s, cublasDgemv(s->cb, CUBLAS_OP_T, n, k + 1, &one, Q, n, w, 1, &zero, s->lh, 1));
+      CB(s, cublasDgemv(s->cb, CUBLAS_OP_N, n, k + 1, &mone, Q, n, s->lh, 1, &one, w, 1));
+    }
+    double beta = 0.0;
+    CB(s, cublasDnrm2(s->cb, n, w, 1, &beta));
+    if (s->fail) return false;
+    al.push_back(alpha);
+    double znorm = 0.0;
+    const double theta = tridiag_min(al, be, k + 1, &znorm);
+    if (k + 1 == n || beta <= 1e-300) { *out = theta; return true; }
+    const double resid = beta * tridiag_last_component(al, be, k + 1, theta, znorm);
+    if (resid <= 1e-12 * std::max(znorm, 1e-300)) { *out = theta; return true; }
+    be.push_back(beta);
+    const double inv = 1.0 / beta;
+    CB(s, cublasDscal(s->cb, n, &inv, w, 1));
+    beta_prev = beta;
+  }
+  return false;
+}
+
 // ---- step lengths (src/step.jl:148-228)
 // slot of lambda_min(L^-1 D L^-T) (src/step.jl:150-163)
 int eigmin_congruence(S* s, Blk& b, const double* L, const double* D) {
@@ -740,6 +891,14 @@ int eigmin_congruence(S* s, Blk& b, const double* L, const double* D) {
   CB(s, cublasDtrsm(s->cb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, n, &one, L,
                     n, b.T1, n));
   LAUNCH(s, k_sym, (int64_t)n * n, n, b.T1);
+  if (n >= kLanczosMin) {
+    double lam = 0.0;
+    if (lanczos_eigmin(s, n, b.T1, &lam)) {
+      const int slot = s->nslot++;
+      CU(s, cudaMemcpyAsync(s->slots + slot, &lam, sizeof(double), cudaMemcpyHostToDevice, s->st));
+      return slot;
+    }
+  }
   const int k = next_info(s);
   CS(s, cusolverDnDsyevd(s->cs, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_LOWER, n, b.T1, n, b.w, s->work, s->lwork,
                          s->dinfo + k));
@@ -747,6 +906,8 @@ int eigmin_congruence(S* s, Blk& b, const double* L, const double* D) {
 }
 
 double eigen_step(double lam, double tau) { return lam > -std::sqrt(kEps) ? 1.0 : std::min(1.0, -tau / lam); }
+
+
 
 // CholeskyBacktrack (src/step.jl:202-221)
 bool backtrack(S* s, bool primal, double* out) {
@@ -854,6 +1015,8 @@ bool take_step(S* s, double a, double bt) {
 
 bool start_iteration(S* s, bool* ok) {
   bool p = false, f = false;
+  s->nev = 0;
+  mark(s, PH_PREPARE);
   if (!prepare(s, &p)) return false;
   if (p && !factorize_schur(s, &f)) return false;
   *ok = p && f;
@@ -870,16 +1033,24 @@ bool iterate_mehrotra(S* s) {
   if (!total_complementarity(s, &tc)) return false;
   const double mu = tc / std::max(nu(s), 1);
   s->mu = mu;
+  mark(s, PH_DIRECTIONS);
   solve_directions(s, 0.0, false);
   double aa = 0, ba = 0, mua = 0;
+  mark(s, PH_STEP);
   if (!step_lengths(s, &aa, &ba) || !affine_complementarity(s, aa, ba, &mua)) return false;
   const double sigma = std::min(std::max(std::pow(mua / std::max(mu, kEps), s->comp.sigma_exponent), 1e-8), 1.0);
   s->sigma = sigma;
+  mark(s, PH_CORRECTION);
   correction(s);
+  mark(s, PH_DIRECTIONS);
   solve_directions(s, sigma * mu, true);
   double a = 0, bt = 0;
+  mark(s, PH_STEP);
   if (!step_lengths(s, &a, &bt)) return false;
-  return take_step(s, a, bt);
+  mark(s, PH_STEP_UPDATE);
+  const bool r = take_step(s, a, bt);
+  collect_marks(s);
+  return r;
 }
 
 // src/primal_dual.jl:104-121
@@ -897,6 +1068,7 @@ bool iterate_adaptive(S* s) {
   if (a + bt > 1.6) mu *= 0.75;
   if (a + bt > 1.9) mu /= 1.0 + 0.1 * s->iter;
   s->mu = mu;
+  collect_marks(s);
   return true;
 }
 
@@ -995,6 +1167,8 @@ int initialize(S* s) {
 
 void release(S* s) {
   if (s->st) cudaStreamSynchronize(s->st);
+  for (auto& e : s->ev)
+    if (e) cudaEventDestroy(e);
   for (void* p : s->allocs) cudaFree(p);
   s->allocs.clear();
   if (s->hslots) cudaFreeHost(s->hslots);
@@ -1040,6 +1214,8 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
     return bail(MSDP_ERR_CUDA);
   cublasSetStream(s->cb, s->st);
   cusolverDnSetStream(s->cs, s->st);
+  for (auto& e : s->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) e = nullptr;
   // ---- host staging of the constraints
   s->B.resize(s->nb);
   double cmax = 0.0;
@@ -1157,6 +1333,13 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   s->lwork = std::max(lwork, 1);
   s->work = vec(s->lwork);
   if (!s->work) return bail(MSDP_ERR_OUT_OF_MEMORY);
+  int nmax = 0;
+  for (auto& b : s->B) nmax = std::max(nmax, b.n);
+  if (nmax >= kLanczosMin) {
+    s->lq = vec((int64_t)nmax * (kLanczosMax + 1));
+    s->lh = vec(kLanczosMax + 1);
+    if (!s->lq || !s->lh) return bail(MSDP_ERR_OUT_OF_MEMORY);
+  }
   double bn = 0.0, dn = 0.0;
   for (int j = 0; j < m; ++j) bn = std::max(bn, std::fabs(d->b[j]));
   for (int k = 0; k < ns; ++k) dn = std::max(dn, std::fabs(d->d_lin[k]));
@@ -1194,6 +1377,7 @@ int msdp_solver_set_initial_point(msdp_solver* s, const double* const* X, const 
 int msdp_solver_solve(msdp_solver* s) {
   if (!s) return MSDP_ERR_INVALID_ARGUMENT;
   s->fail = 0;
+  for (auto& v : s->phase_s) v = 0.0;
   const double t0 = now_s();
   int rc = initialize(s);
   if (rc) return rc;
@@ -1235,6 +1419,15 @@ int msdp_solver_get_trajectory(const msdp_solver* s, msdp_iter_record* out, int3
   for (int32_t k = 0; out && k < capacity && k < *count; ++k) out[k] = s->traj[k];
   return MSDP_OK;
 }
+
+int msdp_solver_get_profile(const msdp_solver* s, double* seconds, int32_t capacity) {
+  if (!s || !seconds) return MSDP_ERR_INVALID_ARGUMENT;
+  const int n = std::min<int>(capacity, PH_COUNT);
+  for (int k = 0; k < n; ++k) seconds[k] = s->phase_s[k];
+  return n;
+}
+
+const char* msdp_solver_profile_field_name(int32_t i) { return (i >= 0 && i < PH_COUNT) ? kPhaseNames[i] : nullptr; }
 
 int64_t msdp_solver_device_bytes(const msdp_solver* s) { return s ? s->bytes : 0; }
 int64_t msdp_solver_launch_count(const msdp_solver* s) { return s ? s->launches : 0; }

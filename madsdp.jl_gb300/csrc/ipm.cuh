@@ -27,8 +27,9 @@ struct SharedState {
   int flag;
   int counter;
   int prob;
-  int pad;
+  int stop;
   double bc[8];  // broadcast scalars
+  uint64_t t0;   // launch start on this CTA (globaltimer)
 };
 
 __device__ __forceinline__ uint64_t globaltimer_ns() {
@@ -1219,7 +1220,7 @@ struct Algo {
       step_lengths(a, bt);
       PROF_END(st, SC_T_STEP);
     }
-    if (!strict && !(fmin(a, bt) >= 0.2)) return false;
+    if (!strict && (!(fmin(a, bt) >= 0.2) || !step_keeps_interior(a, bt))) return false;
     PROF_BEGIN(tk);
     take_step(a, bt);
     PROF_END(tk, SC_T_TAKE);
@@ -1234,7 +1235,7 @@ struct Algo {
     if (!strict && inexact_direction()) return false;
     double a, bt;
     step_lengths(a, bt);
-    if (!strict && !(fmin(a, bt) >= 0.2)) return false;
+    if (!strict && (!(fmin(a, bt) >= 0.2) || !step_keeps_interior(a, bt))) return false;
     take_step(a, bt);
     double mu = prm.ratio * total_complementarity() / fmax((double)nu(), 1.0);
     if (fmin(a, bt) < 0.5) mu *= 1.5;
@@ -1242,6 +1243,18 @@ struct Algo {
     if (a + bt > 1.9) mu /= 1.0 + 0.1 * P.sc[SC_ITER];
     if (threadIdx.x == 0) P.sc[SC_MU] = mu;
     __syncthreads();
+    return true;
+  }
+
+  // A step whose lengths came from compute-type (FP32) factors is taken
+  // only if X + a dX and S + b dS are positive definite in float64: with
+  // cond(S) near 1/eps_f32 the FP32 eigenvalue bound can overshoot.
+  __noinline__ __device__ bool step_keeps_interior(double a, double bt) {
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      if (!add_mul_posdef<double>(b.n, b.X, a, b.dX, b.Shat, smem, sh)) return false;
+      if (!add_mul_posdef<double>(b.n, b.S, bt, b.dS, b.Shat, smem, sh)) return false;
+    }
     return true;
   }
 

@@ -229,8 +229,27 @@ __device__ void run_op(const BatchDev& B, Prob& P, unsigned char* smem, SharedSt
       break;
     }
     case OP_ITERATE: {
+      bool counted = false;  // this problem's first iteration reported to wave_pending
       for (int k = 0; (prm.max_iterations <= 0 || k < prm.max_iterations) && k < 1000000; ++k) {
+        if (k > 0 && B.wave_pending && !counted) {
+          if (threadIdx.x == 0) atomicSub(B.wave_pending, 1);
+          counted = true;
+        }
         if ((int)P.sc[SC_STATUS] != MSDP_REGULAR) break;
+        if (k > 0 && prm.wave_ns > 0.0) {
+          // time-sliced waves: at least one iteration, then stop once the
+          // launch has run wave_ns and every problem of the launch has run
+          // its first iteration (decided by thread 0 for the whole CTA; no
+          // waiting: until then the CTA keeps iterating its own problem)
+          if (threadIdx.x == 0) {
+            const bool late = (double)(globaltimer_ns() - sh.t0) >= prm.wave_ns;
+            sh.stop = late && (!B.wave_pending || atomicAdd(B.wave_pending, 0) <= 0);
+          }
+          __syncthreads();
+          const int stop = sh.stop;
+          __syncthreads();
+          if (stop) break;
+        }
         const long long t_it = clock64();
         iterate_one<MIXED>(B, P, smem, sh);
         if (threadIdx.x == 0) P.sc[SC_T_ITER] += (double)(clock64() - t_it);
@@ -239,6 +258,7 @@ __device__ void run_op(const BatchDev& B, Prob& P, unsigned char* smem, SharedSt
         update_termination(B, P, smem, sh);
         if (threadIdx.x == 0) P.sc[SC_T_TERM] += (double)(clock64() - t_tm);
       }
+      if (B.wave_pending && !counted && threadIdx.x == 0) atomicSub(B.wave_pending, 1);
       break;
     }
     case OP_UPDATE_RESIDUALS: {
@@ -272,6 +292,7 @@ template <int MIXED>
 __global__ void __launch_bounds__(NTHREADS, 3) msdp_ipm_kernel(const __grid_constant__ BatchDev B) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ SharedState sh;
+  if (threadIdx.x == 0) sh.t0 = globaltimer_ns();
   for (;;) {
     if (threadIdx.x == 0) {
       const int q = atomicAdd(B.queue, 1);

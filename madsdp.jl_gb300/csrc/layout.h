@@ -98,6 +98,7 @@ struct Params {
   int32_t op, max_iterations;
   double op_mu;
   int32_t op_corrected, pad;
+  double wave_ns;  // OP_ITERATE: stop a problem's iterations once this long after the launch began (0: no limit)
 };
 
 enum { OP_INITIALIZE = 0, OP_ITERATE = 1, OP_UPDATE_RESIDUALS = 2, OP_PREPARE = 3,
@@ -118,5 +119,9 @@ struct BatchDev {
   const double* p_val;
   const int64_t* ptr;     // conptr / posptr arena
   int32_t* queue;         // work counter
+  // time-sliced waves (OP_ITERATE with prm.wave_ns > 0): problems of this
+  // launch that have not yet run their first iteration; a CTA keeps
+  // iterating its problem past the time budget until this reaches zero
+  int32_t* wave_pending;
   Params prm;
 };

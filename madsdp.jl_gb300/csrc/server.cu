@@ -229,6 +229,7 @@ struct msdp_server {
   BlockDesc* dblk = nullptr;
   int32_t* dorder = nullptr;
   int32_t* queue = nullptr;
+  int32_t* pending_ctr = nullptr;
   double* scal = nullptr;
   int32_t* dslots = nullptr;
   std::vector<int> free_slots;
@@ -338,12 +339,13 @@ int msdp_server_create(msdp_context* ctx, const msdp_components* comp, const msd
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->dorder, sizeof(int32_t) * max_slots);
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->dslots, sizeof(int32_t) * max_slots);
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->queue, sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&s->pending_ctr, sizeof(int32_t));
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->scal, sizeof(double) * max_slots * SC_COUNT);
   if (e == cudaSuccess) e = cudaMemsetAsync(s->dprob, 0, sizeof(ProbDesc) * max_slots, s->stream);
   if (e != cudaSuccess) {
     msdp_server* raw = s.release();
     cudaFree(raw->arena); cudaFree(raw->dprob); cudaFree(raw->dblk); cudaFree(raw->dorder);
-    cudaFree(raw->dslots); cudaFree(raw->queue); cudaFree(raw->scal);
+    cudaFree(raw->dslots); cudaFree(raw->queue); cudaFree(raw->pending_ctr); cudaFree(raw->scal);
     cudaFree(raw->erow); cudaFree(raw->ecol); cudaFree(raw->pcon); cudaFree(raw->eval); cudaFree(raw->pval);
     delete raw;
     return e == cudaErrorMemoryAllocation ? MSDP_ERR_OUT_OF_MEMORY : MSDP_ERR_CUDA;
@@ -361,7 +363,7 @@ int msdp_server_destroy(msdp_server* s) {
   // cudaFree waits for the device; the context's stream is not touched, so
   // a server may outlive its context
   cudaFree(s->arena); cudaFree(s->dprob); cudaFree(s->dblk); cudaFree(s->dorder);
-  cudaFree(s->dslots); cudaFree(s->queue); cudaFree(s->scal);
+  cudaFree(s->dslots); cudaFree(s->queue); cudaFree(s->pending_ctr); cudaFree(s->scal);
   cudaFree(s->erow); cudaFree(s->ecol); cudaFree(s->pcon); cudaFree(s->eval); cudaFree(s->pval);
   delete s;
   return MSDP_OK;
@@ -380,8 +382,9 @@ int msdp_server_submit(msdp_server* s, const msdp_problem_desc* prob, int64_t* r
   return MSDP_OK;
 }
 
-int msdp_server_step(msdp_server* s, int32_t iterations, int32_t* n_active, int32_t* n_completed) {
-  if (!s || iterations <= 0) return MSDP_ERR_INVALID_ARGUMENT;
+int msdp_server_step_budget(msdp_server* s, int32_t iterations, double budget_s, int32_t* n_active,
+                            int32_t* n_completed) {
+  if (!s || iterations <= 0 || !(budget_s >= 0.0)) return MSDP_ERR_INVALID_ARGUMENT;
   cudaStream_t st = s->stream;
   cudaError_t e = cudaSuccess;
   // ---- admission: arrival order, every pending request whose region fits
@@ -439,6 +442,12 @@ int msdp_server_step(msdp_server* s, int32_t iterations, int32_t* n_active, int3
     BatchDev B = server_dev(s, (int)act.size());
     B.prm.op = OP_ITERATE;
     B.prm.max_iterations = iterations;
+    B.prm.wave_ns = budget_s * 1e9;
+    if (budget_s > 0.0) {
+      const int32_t cnt = (int32_t)act.size();
+      if (e == cudaSuccess) e = cudaMemcpyAsync(s->pending_ctr, &cnt, sizeof(int32_t), cudaMemcpyHostToDevice, st);
+      B.wave_pending = s->pending_ctr;
+    }
     int sm = 0, occ = msdp_ipm_occupancy(s->mixed ? 1 : 0);
     cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, 0);
     const int grid = std::min((int)act.size(), std::max(1, sm * std::max(occ, 1)));
@@ -502,6 +511,10 @@ int msdp_server_step(msdp_server* s, int32_t iterations, int32_t* n_active, int3
   }
   if (n_completed) *n_completed = done_now;
   return MSDP_OK;
+}
+
+int msdp_server_step(msdp_server* s, int32_t iterations, int32_t* n_active, int32_t* n_completed) {
+  return msdp_server_step_budget(s, iterations, 0.0, n_active, n_completed);
 }
 
 int msdp_server_counts(const msdp_server* s, int32_t* pending, int32_t* active, int64_t* completed) {

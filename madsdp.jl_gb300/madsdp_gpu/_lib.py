@@ -96,6 +96,7 @@ SIGNATURES = [
     ("msdp_server_destroy", i32, [C.c_void_p]),
     ("msdp_server_submit", i32, [C.c_void_p, P(ProblemDesc), P(i64)]),
     ("msdp_server_step", i32, [C.c_void_p, i32, P(i32), P(i32)]),
+    ("msdp_server_step_budget", i32, [C.c_void_p, i32, f64, P(i32), P(i32)]),
     ("msdp_server_counts", i32, [C.c_void_p, P(i32), P(i32), P(i64)]),
     ("msdp_server_result", i32, [C.c_void_p, i64, P(Stats), P(P(f64)), P(f64), P(f64), P(f64), P(f64)]),
     ("msdp_server_finished", i32, [C.c_void_p, P(i64), i32, P(i32)]),
@@ -110,6 +111,8 @@ SIGNATURES = [
     ("msdp_solver_get_solution", i32, [C.c_void_p, P(P(f64)), P(f64), P(f64), P(f64)]),
     ("msdp_solver_get_trajectory", i32, [C.c_void_p, P(IterRecord), i32, P(i32)]),
     ("msdp_solver_device_bytes", i64, [C.c_void_p]),
+    ("msdp_solver_get_profile", i32, [C.c_void_p, P(f64), i32]),
+    ("msdp_solver_profile_field_name", C.c_char_p, [i32]),
     ("msdp_solver_launch_count", i64, [C.c_void_p]),
     ("msdp_solver_last_error", C.c_char_p, [C.c_void_p]),
 ]

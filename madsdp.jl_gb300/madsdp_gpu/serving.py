@@ -64,9 +64,12 @@ class Server:
         self.models[rid.value] = model
         return rid.value
 
-    def step(self, iterations: int = 2) -> Tuple[int, int]:
+    def step(self, iterations: int = 2, budget_s: float = 0.0) -> Tuple[int, int]:
+        """One wave: admit, initialize newcomers, then up to `iterations`
+        iterations per active request (stopping after `budget_s` seconds
+        of the wave once each has run one, when budget_s > 0)."""
         act, done = C.c_int32(), C.c_int32()
-        rc = self.lib.msdp_server_step(self.h, int(iterations), C.byref(act), C.byref(done))
+        rc = self.lib.msdp_server_step_budget(self.h, int(iterations), float(budget_s), C.byref(act), C.byref(done))
         if rc != 0:
             raise RuntimeError(f"msdp_server_step: {_lib.ERRORS.get(rc, rc)}")
         return act.value, done.value
@@ -111,13 +114,13 @@ class Server:
             if cnt.value < capacity:
                 return out
 
-    def drain(self, iterations: int = 2, max_steps: int = 100000) -> None:
+    def drain(self, iterations: int = 2, max_steps: int = 100000, budget_s: float = 0.0) -> None:
         """Step until nothing is pending or active."""
         for _ in range(max_steps):
             p, a, _ = self.counts()
             if p == 0 and a == 0:
                 return
-            self.step(iterations)
+            self.step(iterations, budget_s)
         raise RuntimeError("server did not drain")
 
 
@@ -156,10 +159,11 @@ def poisson_stream(rate: float, duration: float, seed: int = 0, sos_d=(5, 63), m
 
 
 def serve_stream(server: Server, stream: Sequence[Tuple[float, str, Model]], iterations: int = 2,
-                 time_limit: float = 600.0) -> dict:
+                 time_limit: float = 600.0, budget_s: float = 0.0) -> dict:
     """Replay `stream` in real time: requests are submitted when their arrival
-    time has passed, the server steps continuously.  Latency = finish time -
-    arrival time (host clock)."""
+    time has passed, the server steps continuously (waves of `iterations`
+    iterations, time-sliced by `budget_s` when positive).  Latency = finish
+    time - arrival time (host clock)."""
     t0 = time.perf_counter()
     nxt, ids = 0, {}
     lat, kinds, statuses = [], [], []
@@ -170,7 +174,7 @@ def serve_stream(server: Server, stream: Sequence[Tuple[float, str, Model]], ite
             nxt += 1
         p, a, _ = server.counts()
         if p or a:
-            server.step(iterations)
+            server.step(iterations, budget_s)
         elif nxt < len(stream):
             time.sleep(min(0.002, max(0.0, stream[nxt][0] - now)))
         t_after = time.perf_counter() - t0
@@ -186,6 +190,15 @@ def serve_stream(server: Server, stream: Sequence[Tuple[float, str, Model]], ite
             raise RuntimeError("serving did not finish within the time limit")
     wall = time.perf_counter() - t0
     lat = np.array(lat)
+    by_kind = {}
+    for k, st, l in zip(kinds, statuses, lat):
+        d = by_kind.setdefault(k, {"n": 0, "succeeded": 0, "lat": []})
+        d["n"] += 1
+        d["succeeded"] += int(st == Status.SOLVE_SUCCEEDED)
+        d["lat"].append(l)
+    per_kind = {k: {"requests": d["n"], "succeeded": d["succeeded"],
+                    "p50_latency_ms": float(np.percentile(d["lat"], 50) * 1e3),
+                    "p99_latency_ms": float(np.percentile(d["lat"], 99) * 1e3)} for k, d in by_kind.items()}
     return {
         "requests": len(stream), "completed": len(lat), "wall_s": wall,
         "solves_per_s": len(lat) / wall,
@@ -193,4 +206,7 @@ def serve_stream(server: Server, stream: Sequence[Tuple[float, str, Model]], ite
         "p99_latency_ms": float(np.percentile(lat, 99) * 1e3) if len(lat) else None,
         "succeeded": int(sum(1 for s in statuses if s == Status.SOLVE_SUCCEEDED)),
         "launches": server.launch_count,
+        "per_kind": per_kind,
+        "statuses": {str(k): int(v) for k, v in zip(*np.unique([int(x) for x in statuses], return_counts=True))}
+        if statuses else {},
     }

@@ -447,6 +447,12 @@ class InstanceSolver:
     def launch_count(self) -> int:
         return int(self.lib.msdp_solver_launch_count(self.h))
 
+    def profile(self) -> dict:
+        """Device seconds per phase of the last solve."""
+        buf = (C.c_double * 16)()
+        n = self.lib.msdp_solver_get_profile(self.h, buf, 16)
+        return {self.lib.msdp_solver_profile_field_name(i).decode(): buf[i] for i in range(max(n, 0))}
+
     def stats(self) -> dict:
         st = _lib.Stats()
         self.lib.msdp_solver_get_stats(self.h, C.byref(st))

@@ -70,6 +70,13 @@ def test_maxcut_pm1_weights_large(gpu_ctx):
     assert_matches_oracle(inst(model), o.Solver(model).solve())
 
 
+def test_lanczos_step_lengths_hkm(gpu_ctx):
+    """Blocks of 257 and more take lambda_min by Lanczos; HKM exercises both
+    the primal (Lx) and dual (Ls) congruences."""
+    model = g.maxcut(300, 0.03, seed=8)
+    assert_matches_oracle(inst(model, direction=M.HKM()), o.Solver(model, direction=o.HKM()).solve())
+
+
 @pytest.mark.parametrize("direction", ["NT", "HKM"])
 def test_dense_mixed_cones(gpu_ctx, direction):
     """Dense A with two PSD blocks and scalars: the GEMM assembly path."""

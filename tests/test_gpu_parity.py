@@ -190,6 +190,22 @@ def test_sos_batch_mixed(gpu_ctx):
         assert st["iter_fp32"] >= 1
 
 
+def test_mixed_late_fp32_steps_stay_interior(gpu_ctx):
+    """Near convergence, with cond(S) close to 1/eps_f32, a step length from
+    FP32 factors can overshoot the PSD boundary; such steps are checked in
+    float64 before they are taken (max-cut requests of the served stream
+    that ended in ERROR_IN_STEP_COMPUTATION without the check)."""
+    from madsdp_gpu.serving import poisson_stream
+    st = poisson_stream(200.0, 1.0, seed=21, sos_d=(5, 127), maxcut_n=(20, 100), dense_n=(8, 32), dense_m=200)
+    mc = [m for _, k, m in st if k == "maxcut"]
+    assert len(mc) >= 34
+    bt = M.Batch(mc, precision="mixed")
+    bt.solve()
+    for i, s in enumerate(bt.all_stats()):
+        assert s["status"] == M.Status.SOLVE_SUCCEEDED, (i, s)
+        assert max(s["inf_pr"], s["inf_du"], s["gap"]) <= 1e-7
+
+
 def test_batch_uneven_results_independent_of_mix(gpu_ctx):
     """A problem's result is the same alone and inside an uneven batch."""
     models = [g.sos_hankel(7, seed=5), g.maxcut(30, 0.2, seed=3), g.sos_hankel(20, seed=6),

@@ -56,12 +56,12 @@ def test_server_matches_solving_alone(gpu_ctx):
     srv.close()
 
 
-@pytest.mark.parametrize("iterations", [1, 7])
-def test_server_wave_length_does_not_change_results(gpu_ctx, iterations):
+@pytest.mark.parametrize("iterations,budget_s", [(1, 0.0), (7, 0.0), (1000, 0.002)])
+def test_server_wave_length_does_not_change_results(gpu_ctx, iterations, budget_s):
     models = mixed_requests()[:4]
     srv = Server(memory_budget_bytes=32 << 20, max_slots=8)
     ids = [srv.submit(m) for m in models]
-    srv.drain(iterations)
+    srv.drain(iterations, budget_s=budget_s)
     for rid, m in zip(ids, models):
         st, X, y = alone(m)
         assert_same(srv.result(rid), st, X, y)
@@ -114,7 +114,7 @@ def test_server_mixed_precision(gpu_ctx):
 def test_serve_poisson_stream(gpu_ctx):
     stream = poisson_stream(rate=400.0, duration=0.1, seed=3, sos_d=(5, 20), maxcut_n=(20, 30), dense_n=(6, 10))
     srv = Server(memory_budget_bytes=256 << 20, max_slots=64)
-    out = serve_stream(srv, stream, iterations=2, time_limit=120.0)
+    out = serve_stream(srv, stream, iterations=1000, time_limit=120.0, budget_s=0.005)
     assert out["completed"] == out["requests"] == len(stream) > 0
     assert out["succeeded"] == out["completed"]
     assert out["p99_latency_ms"] >= out["p50_latency_ms"] > 0
