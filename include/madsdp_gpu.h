@@ -227,9 +227,14 @@ int msdp_server_destroy(msdp_server* server);
 /* Copies the problem; returns MSDP_ERR_TOO_LARGE if it can never fit. */
 int msdp_server_submit(msdp_server* server, const msdp_problem_desc* problem, int64_t* request_id);
 int msdp_server_step(msdp_server* server, int32_t iterations, int32_t* active, int32_t* completed);
-/* Time-sliced wave: every active request runs at least one and at most
- * `iterations` iterations, stopping once the wave has run `budget_s` seconds,
- * so small requests finish within one wave while large ones progress. */
+/* Asynchronous, time-sliced waves: collects the waves that have finished
+ * (their terminated requests become results), admits pending requests, and
+ * starts one wave over every idle request on a free stream of the server
+ * without waiting for it, so waves overlap on the GPU and new requests do
+ * not wait for long-running ones.  Within a wave each request runs at least
+ * one and at most `iterations` iterations, stopping once the wave has run
+ * `budget_s` seconds and every request of the wave has iterated once.
+ * msdp_server_step is the synchronous form (budget 0, waits for the wave). */
 int msdp_server_step_budget(msdp_server* server, int32_t iterations, double budget_s, int32_t* active,
                             int32_t* completed);
 int msdp_server_counts(const msdp_server* server, int32_t* pending, int32_t* active, int64_t* completed);

@@ -203,6 +203,7 @@ struct Request {
   int slot = -1;
   int64_t region = -1;
   int64_t entries = -1;
+  int wave = -1;  // wave the request is running in, -1 when idle
   bool done = false;
   msdp_stats stats{};
   std::vector<std::vector<double>> X;
@@ -211,12 +212,27 @@ struct Request {
 
 }  // namespace
 
+// One wave: a persistent launch over a set of requests on its own stream.
+// Waves overlap on the device; a request belongs to at most one running
+// wave, and the host only touches a wave's requests after its event.
+constexpr int kWaves = 16;
+
+struct Wave {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  int32_t *dorder = nullptr, *dinit = nullptr, *queue = nullptr, *pending = nullptr;
+  double* scal = nullptr;   // device scalars of the wave's requests
+  double* hscal = nullptr;  // pinned host copy
+  std::vector<int32_t> slots;
+  bool busy = false;
+};
+
 struct msdp_server {
   msdp_context* ctx = nullptr;
-  cudaStream_t stream = nullptr;
   Params prm{};
   bool mixed = false;
   int capacity = 0;
+  int sm_count = 0, occupancy = 1;
   unsigned char* arena = nullptr;
   int64_t arena_bytes = 0;
   std::map<int64_t, int64_t> free_blocks;  // main arena: offset -> size (bytes)
@@ -227,11 +243,7 @@ struct msdp_server {
   std::map<int64_t, int64_t> free_entries;  // index -> count
   ProbDesc* dprob = nullptr;
   BlockDesc* dblk = nullptr;
-  int32_t* dorder = nullptr;
-  int32_t* queue = nullptr;
-  int32_t* pending_ctr = nullptr;
-  double* scal = nullptr;
-  int32_t* dslots = nullptr;
+  Wave waves[kWaves];
   std::vector<int> free_slots;
   std::deque<std::unique_ptr<Request>> pending;
   std::vector<Request*> active;              // by slot
@@ -277,116 +289,110 @@ void list_free(std::map<int64_t, int64_t>& fl, int64_t off, int64_t size) {
   }
 }
 
-BatchDev server_dev(msdp_server* s, int count) {
+BatchDev server_dev(msdp_server* s, const Wave& w, const int32_t* order, int count) {
   BatchDev B;
   std::memset(&B, 0, sizeof(B));
   B.nprob = count;
-  B.prob = s->dprob; B.blk = s->dblk; B.order = s->dorder;
+  B.prob = s->dprob; B.blk = s->dblk; B.order = order;
   B.dd = (const double*)s->arena; B.d64 = (double*)s->arena; B.d32 = (float*)s->arena;
   B.e_row = s->erow; B.e_col = s->ecol; B.e_val = s->eval;
   B.p_con = s->pcon; B.p_val = s->pval; B.ptr = (const int64_t*)s->arena;
-  B.queue = s->queue;
+  B.queue = w.queue;
   B.prm = s->prm;
   return B;
 }
 
-}  // namespace
-
-extern "C" {
-
-int msdp_server_create(msdp_context* ctx, const msdp_components* comp, const msdp_options* opt,
-                       int64_t memory_budget_bytes, int32_t max_slots, msdp_server** out) {
-  if (!ctx || !out || memory_budget_bytes <= 0 || max_slots <= 0) return MSDP_ERR_INVALID_ARGUMENT;
-  *out = nullptr;
-  msdp_components c;
-  msdp_options o;
-  if (comp) c = *comp; else msdp_default_components(&c);
-  if (opt) o = *opt; else msdp_default_options(&o);
-  if (c.algorithm == MSDP_DUAL_CENTERING || (c.schur == MSDP_QR_SCHUR && c.precision != MSDP_FP64) ||
-      (c.schur == MSDP_QR_SCHUR && c.direction != MSDP_NT) || !(c.shrink > 0.0 && c.shrink < 1.0) ||
-      !(c.boundary > 0.0 && c.boundary <= 1.0) || !(c.tau > 0.0) || o.max_iter < 0 ||
-      (c.initial_point == MSDP_INITIAL_POINT) || (c.initial_point == MSDP_DUAL_SHIFT && !(c.initial_shift > 0.0)))
-    return MSDP_ERR_INVALID_ARGUMENT;
-  auto s = std::make_unique<msdp_server>();
-  s->ctx = ctx;
-  s->stream = (cudaStream_t)msdp_context_stream(ctx);
-  s->mixed = (c.precision == MSDP_MIXED);
-  s->capacity = max_slots;
-  Params& prm = s->prm;
-  prm.algorithm = c.algorithm; prm.direction = c.direction; prm.step = c.step; prm.centering = c.centering;
-  prm.initial_point = c.initial_point; prm.schur = c.schur; prm.precision = c.precision;
-  prm.centering_max_iter = c.centering_max_iter;
-  prm.tau = c.tau; prm.shrink = c.shrink; prm.boundary = c.boundary; prm.sigma_exponent = c.sigma_exponent;
-  prm.initial_ratio = c.initial_ratio; prm.ratio = c.ratio; prm.scale = c.scale;
-  prm.initial_shift = c.initial_shift; prm.max_shift = c.max_shift;
-  prm.dc_beta = c.dc_beta; prm.dc_delta = c.dc_delta; prm.dc_A = c.dc_A;
-  prm.tol = o.tol; prm.max_wall_time = o.max_wall_time; prm.mu_min = o.mu_min;
-  prm.regularize_schur = o.regularize_schur; prm.switch_tol = o.switch_tol;
-  prm.max_iter = o.max_iter; prm.max_schur_reg = o.max_schur_reg;
-  prm.mixed_refine = std::max(0, std::min(o.mixed_refine, 8));
-  // three quarters of the budget for the main arena, one quarter for the
-  // constraint entries (28 bytes per entry over the five arrays)
-  s->arena_bytes = a256(memory_budget_bytes / 4 * 3);
-  s->entry_capacity = std::max<int64_t>(1, (memory_budget_bytes / 4) / 28);
-  cudaError_t e = cudaMalloc((void**)&s->arena, (size_t)s->arena_bytes);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->erow, sizeof(int32_t) * s->entry_capacity);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->ecol, sizeof(int32_t) * s->entry_capacity);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->pcon, sizeof(int32_t) * s->entry_capacity);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->eval, sizeof(double) * s->entry_capacity);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->pval, sizeof(double) * s->entry_capacity);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->dprob, sizeof(ProbDesc) * max_slots);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->dblk, sizeof(BlockDesc) * max_slots * kMaxBlocks);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->dorder, sizeof(int32_t) * max_slots);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->dslots, sizeof(int32_t) * max_slots);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->queue, sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->pending_ctr, sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->scal, sizeof(double) * max_slots * SC_COUNT);
-  if (e == cudaSuccess) e = cudaMemsetAsync(s->dprob, 0, sizeof(ProbDesc) * max_slots, s->stream);
-  if (e != cudaSuccess) {
-    msdp_server* raw = s.release();
-    cudaFree(raw->arena); cudaFree(raw->dprob); cudaFree(raw->dblk); cudaFree(raw->dorder);
-    cudaFree(raw->dslots); cudaFree(raw->queue); cudaFree(raw->pending_ctr); cudaFree(raw->scal);
-    cudaFree(raw->erow); cudaFree(raw->ecol); cudaFree(raw->pcon); cudaFree(raw->eval); cudaFree(raw->pval);
-    delete raw;
-    return e == cudaErrorMemoryAllocation ? MSDP_ERR_OUT_OF_MEMORY : MSDP_ERR_CUDA;
+void free_server(msdp_server* s) {
+  for (auto& w : s->waves) {
+    if (w.stream) cudaStreamSynchronize(w.stream);
+    cudaFree(w.dorder); cudaFree(w.dinit); cudaFree(w.queue); cudaFree(w.pending); cudaFree(w.scal);
+    if (w.hscal) cudaFreeHost(w.hscal);
+    if (w.done) cudaEventDestroy(w.done);
+    if (w.stream) cudaStreamDestroy(w.stream);
   }
-  s->free_blocks[0] = s->arena_bytes;
-  s->free_entries[0] = s->entry_capacity;
-  s->active.assign(max_slots, nullptr);
-  for (int k = max_slots - 1; k >= 0; --k) s->free_slots.push_back(k);
-  *out = s.release();
-  return MSDP_OK;
-}
-
-int msdp_server_destroy(msdp_server* s) {
-  if (!s) return MSDP_OK;
-  // cudaFree waits for the device; the context's stream is not touched, so
-  // a server may outlive its context
-  cudaFree(s->arena); cudaFree(s->dprob); cudaFree(s->dblk); cudaFree(s->dorder);
-  cudaFree(s->dslots); cudaFree(s->queue); cudaFree(s->pending_ctr); cudaFree(s->scal);
+  cudaFree(s->arena); cudaFree(s->dprob); cudaFree(s->dblk);
   cudaFree(s->erow); cudaFree(s->ecol); cudaFree(s->pcon); cudaFree(s->eval); cudaFree(s->pval);
-  delete s;
-  return MSDP_OK;
 }
 
-int msdp_server_submit(msdp_server* s, const msdp_problem_desc* prob, int64_t* request_id) {
-  if (!s || !prob || !request_id) return MSDP_ERR_INVALID_ARGUMENT;
-  auto r = std::make_unique<Request>();
-  const int rc = stage_problem(*prob, s->prm, s->mixed, r->st);
-  if (rc) return rc;
-  if (r->st.total_bytes > s->arena_bytes || r->st.nnz > s->entry_capacity) return MSDP_ERR_TOO_LARGE;
-  r->id = s->next_id++;
-  r->t_submit = now_s();
-  *request_id = r->id;
-  s->pending.push_back(std::move(r));
-  return MSDP_OK;
-}
-
-int msdp_server_step_budget(msdp_server* s, int32_t iterations, double budget_s, int32_t* n_active,
-                            int32_t* n_completed) {
-  if (!s || iterations <= 0 || !(budget_s >= 0.0)) return MSDP_ERR_INVALID_ARGUMENT;
-  cudaStream_t st = s->stream;
+// Results of a finished wave: requests that terminated are copied to the
+// host and leave the arena; the others become idle for the next wave.
+cudaError_t harvest_wave(msdp_server* s, Wave& w, int* done_now) {
   cudaError_t e = cudaSuccess;
+  std::vector<Request*> fin;
+  for (size_t q = 0; q < w.slots.size(); ++q) {
+    const double* v = w.hscal + q * SC_COUNT;
+    Request* r = s->active[w.slots[q]];
+    r->wave = -1;
+    const int status = (int)v[SC_STATUS];
+    if (status == MSDP_REGULAR) continue;
+    msdp_stats& o = r->stats;
+    std::memset(&o, 0, sizeof(o));
+    o.status = status == MSDP_STATUS_INITIAL_POINT_ERROR ? MSDP_ERROR_IN_STEP_COMPUTATION : status;
+    o.iter = (int32_t)v[SC_ITER]; o.iter_fp32 = (int32_t)v[SC_N32]; o.iter_fp64 = (int32_t)v[SC_N64];
+    o.pobj = v[SC_POBJ]; o.dobj = v[SC_DOBJ]; o.inf_pr = v[SC_INFPR]; o.inf_du = v[SC_INFDU]; o.gap = v[SC_GAP];
+    o.mu = v[SC_MU]; o.sigma = v[SC_SIGMA]; o.alpha = v[SC_ALPHA]; o.beta = v[SC_BETA]; o.solve_ns = v[SC_SOLVE_NS];
+    const Staged& stg = r->st;
+    const int64_t m = stg.m, ns = stg.ns;
+    r->y.resize(m); r->x.resize(ns); r->z.resize(ns);
+    const double* v64 = (const double*)s->arena + stg.pd.v64;
+    if (e == cudaSuccess && m)
+      e = cudaMemcpyAsync(r->y.data(), v64 + (int64_t)V_Y * m, 8 * m, cudaMemcpyDeviceToHost, w.stream);
+    const double* sv = v64 + (int64_t)V_MCOUNT * m;
+    if (e == cudaSuccess && ns)
+      e = cudaMemcpyAsync(r->x.data(), sv + (int64_t)S_X * ns, 8 * ns, cudaMemcpyDeviceToHost, w.stream);
+    if (e == cudaSuccess && ns)
+      e = cudaMemcpyAsync(r->z.data(), sv + (int64_t)S_Z * ns, 8 * ns, cudaMemcpyDeviceToHost, w.stream);
+    r->X.resize(stg.nblocks);
+    for (int i = 0; i < stg.nblocks; ++i) {
+      const int64_t n = stg.bd[i].n;
+      r->X[i].resize(n * n);
+      const double* Xd = (const double*)s->arena + stg.bd[i].m64 + (int64_t)M_X * n * n;
+      if (e == cudaSuccess) e = cudaMemcpyAsync(r->X[i].data(), Xd, 8 * n * n, cudaMemcpyDeviceToHost, w.stream);
+    }
+    fin.push_back(r);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(w.stream);
+  const double t = now_s();
+  for (Request* r : fin) {
+    r->t_done = t;
+    r->done = true;
+    list_free(s->free_blocks, r->region, r->st.total_bytes);
+    list_free(s->free_entries, r->entries, r->st.nnz);
+    s->active[r->slot] = nullptr;
+    s->free_slots.push_back(r->slot);
+    s->finished.push_back(r->id);
+    ++s->completed;
+    ++*done_now;
+  }
+  w.slots.clear();
+  w.busy = false;
+  return e;
+}
+
+int count_active(const msdp_server* s) {
+  int a = 0;
+  for (auto* r : s->active) a += (r != nullptr);
+  return a;
+}
+
+// Harvest finished waves, admit pending requests, and start one wave over
+// every idle request (on a free wave stream).  Returns without waiting.
+int step_async(msdp_server* s, int32_t iterations, double budget_s, int* done_now) {
+  cudaError_t e = cudaSuccess;
+  for (auto& w : s->waves) {
+    if (!w.busy) continue;
+    const cudaError_t q = cudaEventQuery(w.done);
+    if (q == cudaErrorNotReady) continue;
+    if (q != cudaSuccess) { s->err = cudaGetErrorString(q); return MSDP_ERR_CUDA; }
+    e = harvest_wave(s, w, done_now);
+    if (e != cudaSuccess) { s->err = cudaGetErrorString(e); return MSDP_ERR_CUDA; }
+  }
+  int wi = -1;
+  for (int k = 0; k < kWaves; ++k)
+    if (!s->waves[k].busy) { wi = k; break; }
+  if (wi < 0) return MSDP_OK;  // every wave stream is busy
+  Wave& w = s->waves[wi];
+  cudaStream_t st = w.stream;
   // ---- admission: arrival order, every pending request whose region fits
   std::vector<int32_t> fresh;
   for (auto it = s->pending.begin(); it != s->pending.end();) {
@@ -423,108 +429,183 @@ int msdp_server_step_budget(msdp_server* s, int32_t iterations, double budget_s,
     it = s->pending.erase(it);
   }
   if (e != cudaSuccess) { s->err = cudaGetErrorString(e); return MSDP_ERR_CUDA; }
-  // ---- initialize the newcomers, then one wave over every active request
+  // ---- the wave: every idle request (fresh ones initialized first)
   std::vector<int32_t> act;
   for (int k = 0; k < s->capacity; ++k)
-    if (s->active[k]) act.push_back(k);
+    if (s->active[k] && s->active[k]->wave < 0) act.push_back(k);
+  if (act.empty()) return MSDP_OK;
+  const int mk = s->mixed ? 1 : 0;
   if (!fresh.empty()) {
-    e = cudaMemcpyAsync(s->dorder, fresh.data(), sizeof(int32_t) * fresh.size(), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s->queue, 0, sizeof(int32_t), st);
-    BatchDev B = server_dev(s, (int)fresh.size());
+    e = cudaMemcpyAsync(w.dinit, fresh.data(), sizeof(int32_t) * fresh.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.queue, 0, sizeof(int32_t), st);
+    BatchDev B = server_dev(s, w, w.dinit, (int)fresh.size());
     B.prm.op = OP_INITIALIZE;
-    if (e == cudaSuccess) e = msdp_ipm_launch(s->mixed ? 1 : 0, B, (int)fresh.size(), st);
+    const int grid = std::min((int)fresh.size(), std::max(1, s->sm_count * s->occupancy));
+    if (e == cudaSuccess) e = msdp_ipm_launch(mk, B, grid, st);
     s->launches += 1;
   }
-  if (!act.empty()) {
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(s->dorder, act.data(), sizeof(int32_t) * act.size(), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s->queue, 0, sizeof(int32_t), st);
-    BatchDev B = server_dev(s, (int)act.size());
-    B.prm.op = OP_ITERATE;
-    B.prm.max_iterations = iterations;
-    B.prm.wave_ns = budget_s * 1e9;
-    if (budget_s > 0.0) {
-      const int32_t cnt = (int32_t)act.size();
-      if (e == cudaSuccess) e = cudaMemcpyAsync(s->pending_ctr, &cnt, sizeof(int32_t), cudaMemcpyHostToDevice, st);
-      B.wave_pending = s->pending_ctr;
-    }
-    int sm = 0, occ = msdp_ipm_occupancy(s->mixed ? 1 : 0);
-    cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, 0);
-    const int grid = std::min((int)act.size(), std::max(1, sm * std::max(occ, 1)));
-    if (e == cudaSuccess) e = msdp_ipm_launch(s->mixed ? 1 : 0, B, grid, st);
-    s->launches += 1;
-    // ---- harvest: scalars of the active slots
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(s->dslots, act.data(), sizeof(int32_t) * act.size(), cudaMemcpyHostToDevice, st);
-    BatchDev G = server_dev(s, (int)act.size());
-    if (e == cudaSuccess) e = msdp_gather_launch_idx(G, s->dslots, (int)act.size(), s->scal, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(w.dorder, act.data(), sizeof(int32_t) * act.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.queue, 0, sizeof(int32_t), st);
+  BatchDev B = server_dev(s, w, w.dorder, (int)act.size());
+  B.prm.op = OP_ITERATE;
+  B.prm.max_iterations = iterations;
+  B.prm.wave_ns = budget_s * 1e9;
+  if (budget_s > 0.0) {
+    const int32_t cnt = (int32_t)act.size();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w.pending, &cnt, sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    B.wave_pending = w.pending;
   }
-  std::vector<double> sc(act.size() * SC_COUNT);
-  if (e == cudaSuccess && !act.empty())
-    e = cudaMemcpyAsync(sc.data(), s->scal, sizeof(double) * sc.size(), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  const int grid = std::min((int)act.size(), std::max(1, s->sm_count * s->occupancy));
+  if (e == cudaSuccess) e = msdp_ipm_launch(mk, B, grid, st);
+  s->launches += 1;
+  BatchDev G = server_dev(s, w, w.dorder, (int)act.size());
+  if (e == cudaSuccess) e = msdp_gather_launch_idx(G, w.dorder, (int)act.size(), w.scal, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(w.hscal, w.scal, sizeof(double) * SC_COUNT * act.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaEventRecord(w.done, st);
   if (e != cudaSuccess) { s->err = cudaGetErrorString(e); return MSDP_ERR_CUDA; }
+  for (int32_t k : act) s->active[k]->wave = wi;
+  w.slots = act;
+  w.busy = true;
+  return MSDP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int msdp_server_create(msdp_context* ctx, const msdp_components* comp, const msdp_options* opt,
+                       int64_t memory_budget_bytes, int32_t max_slots, msdp_server** out) {
+  if (!ctx || !out || memory_budget_bytes <= 0 || max_slots <= 0) return MSDP_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  msdp_components c;
+  msdp_options o;
+  if (comp) c = *comp; else msdp_default_components(&c);
+  if (opt) o = *opt; else msdp_default_options(&o);
+  if (c.algorithm == MSDP_DUAL_CENTERING || (c.schur == MSDP_QR_SCHUR && c.precision != MSDP_FP64) ||
+      (c.schur == MSDP_QR_SCHUR && c.direction != MSDP_NT) || !(c.shrink > 0.0 && c.shrink < 1.0) ||
+      !(c.boundary > 0.0 && c.boundary <= 1.0) || !(c.tau > 0.0) || o.max_iter < 0 ||
+      (c.initial_point == MSDP_INITIAL_POINT) || (c.initial_point == MSDP_DUAL_SHIFT && !(c.initial_shift > 0.0)))
+    return MSDP_ERR_INVALID_ARGUMENT;
+  auto s = std::make_unique<msdp_server>();
+  s->ctx = ctx;
+  s->mixed = (c.precision == MSDP_MIXED);
+  s->capacity = max_slots;
+  Params& prm = s->prm;
+  prm.algorithm = c.algorithm; prm.direction = c.direction; prm.step = c.step; prm.centering = c.centering;
+  prm.initial_point = c.initial_point; prm.schur = c.schur; prm.precision = c.precision;
+  prm.centering_max_iter = c.centering_max_iter;
+  prm.tau = c.tau; prm.shrink = c.shrink; prm.boundary = c.boundary; prm.sigma_exponent = c.sigma_exponent;
+  prm.initial_ratio = c.initial_ratio; prm.ratio = c.ratio; prm.scale = c.scale;
+  prm.initial_shift = c.initial_shift; prm.max_shift = c.max_shift;
+  prm.dc_beta = c.dc_beta; prm.dc_delta = c.dc_delta; prm.dc_A = c.dc_A;
+  prm.tol = o.tol; prm.max_wall_time = o.max_wall_time; prm.mu_min = o.mu_min;
+  prm.regularize_schur = o.regularize_schur; prm.switch_tol = o.switch_tol;
+  prm.max_iter = o.max_iter; prm.max_schur_reg = o.max_schur_reg;
+  prm.mixed_refine = std::max(0, std::min(o.mixed_refine, 8));
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  s->occupancy = std::max(1, msdp_ipm_occupancy(s->mixed ? 1 : 0));
+  // three quarters of the budget for the main arena, one quarter for the
+  // constraint entries (28 bytes per entry over the five arrays)
+  s->arena_bytes = a256(memory_budget_bytes / 4 * 3);
+  s->entry_capacity = std::max<int64_t>(1, (memory_budget_bytes / 4) / 28);
+  cudaError_t e = cudaMalloc((void**)&s->arena, (size_t)s->arena_bytes);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&s->erow, sizeof(int32_t) * s->entry_capacity);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&s->ecol, sizeof(int32_t) * s->entry_capacity);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&s->pcon, sizeof(int32_t) * s->entry_capacity);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&s->eval, sizeof(double) * s->entry_capacity);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&s->pval, sizeof(double) * s->entry_capacity);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&s->dprob, sizeof(ProbDesc) * max_slots);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&s->dblk, sizeof(BlockDesc) * max_slots * kMaxBlocks);
+  if (e == cudaSuccess) e = cudaMemset(s->dprob, 0, sizeof(ProbDesc) * max_slots);
+  for (auto& w : s->waves) {
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&w.dorder, sizeof(int32_t) * max_slots);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&w.dinit, sizeof(int32_t) * max_slots);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&w.queue, sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&w.pending, sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&w.scal, sizeof(double) * SC_COUNT * max_slots);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&w.hscal, sizeof(double) * SC_COUNT * max_slots);
+  }
+  if (e != cudaSuccess) {
+    msdp_server* raw = s.release();
+    free_server(raw);
+    delete raw;
+    return e == cudaErrorMemoryAllocation ? MSDP_ERR_OUT_OF_MEMORY : MSDP_ERR_CUDA;
+  }
+  s->free_blocks[0] = s->arena_bytes;
+  s->free_entries[0] = s->entry_capacity;
+  s->active.assign(max_slots, nullptr);
+  for (int k = max_slots - 1; k >= 0; --k) s->free_slots.push_back(k);
+  *out = s.release();
+  return MSDP_OK;
+}
+
+int msdp_server_destroy(msdp_server* s) {
+  if (!s) return MSDP_OK;
+  // the server's own streams are synchronized; the context's stream is not
+  // touched, so a server may outlive its context
+  free_server(s);
+  delete s;
+  return MSDP_OK;
+}
+
+int msdp_server_submit(msdp_server* s, const msdp_problem_desc* prob, int64_t* request_id) {
+  if (!s || !prob || !request_id) return MSDP_ERR_INVALID_ARGUMENT;
+  auto r = std::make_unique<Request>();
+  const int rc = stage_problem(*prob, s->prm, s->mixed, r->st);
+  if (rc) return rc;
+  if (r->st.total_bytes > s->arena_bytes || r->st.nnz > s->entry_capacity) return MSDP_ERR_TOO_LARGE;
+  r->id = s->next_id++;
+  r->t_submit = now_s();
+  *request_id = r->id;
+  s->pending.push_back(std::move(r));
+  return MSDP_OK;
+}
+
+int msdp_server_step_budget(msdp_server* s, int32_t iterations, double budget_s, int32_t* n_active,
+                            int32_t* n_completed) {
+  if (!s || iterations <= 0 || !(budget_s >= 0.0)) return MSDP_ERR_INVALID_ARGUMENT;
   int done_now = 0;
-  for (size_t q = 0; q < act.size(); ++q) {
-    const double* v = sc.data() + q * SC_COUNT;
-    const int status = (int)v[SC_STATUS];
-    if (status == MSDP_REGULAR) continue;
-    Request* r = s->active[act[q]];
-    msdp_stats& o = r->stats;
-    std::memset(&o, 0, sizeof(o));
-    o.status = status == MSDP_STATUS_INITIAL_POINT_ERROR ? MSDP_ERROR_IN_STEP_COMPUTATION : status;
-    o.iter = (int32_t)v[SC_ITER]; o.iter_fp32 = (int32_t)v[SC_N32]; o.iter_fp64 = (int32_t)v[SC_N64];
-    o.pobj = v[SC_POBJ]; o.dobj = v[SC_DOBJ]; o.inf_pr = v[SC_INFPR]; o.inf_du = v[SC_INFDU]; o.gap = v[SC_GAP];
-    o.mu = v[SC_MU]; o.sigma = v[SC_SIGMA]; o.alpha = v[SC_ALPHA]; o.beta = v[SC_BETA]; o.solve_ns = v[SC_SOLVE_NS];
-    // solution to host, then release the region
-    const Staged& stg = r->st;
-    const int64_t m = stg.m, ns = stg.ns;
-    r->y.resize(m); r->x.resize(ns); r->z.resize(ns);
-    const double* v64 = (const double*)s->arena + stg.pd.v64;
-    if (e == cudaSuccess && m) e = cudaMemcpyAsync(r->y.data(), v64 + (int64_t)V_Y * m, 8 * m, cudaMemcpyDeviceToHost, st);
-    const double* sv = v64 + (int64_t)V_MCOUNT * m;
-    if (e == cudaSuccess && ns) e = cudaMemcpyAsync(r->x.data(), sv + (int64_t)S_X * ns, 8 * ns, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess && ns) e = cudaMemcpyAsync(r->z.data(), sv + (int64_t)S_Z * ns, 8 * ns, cudaMemcpyDeviceToHost, st);
-    r->X.resize(stg.nblocks);
-    for (int i = 0; i < stg.nblocks; ++i) {
-      const int64_t n = stg.bd[i].n;
-      r->X[i].resize(n * n);
-      const double* Xd = (const double*)s->arena + stg.bd[i].m64 + (int64_t)M_X * n * n;
-      if (e == cudaSuccess) e = cudaMemcpyAsync(r->X[i].data(), Xd, 8 * n * n, cudaMemcpyDeviceToHost, st);
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    r->t_done = now_s();
-    r->done = true;
-    list_free(s->free_blocks, r->region, stg.total_bytes);
-    list_free(s->free_entries, r->entries, stg.nnz);
-    s->active[act[q]] = nullptr;
-    s->free_slots.push_back(act[q]);
-    s->finished.push_back(r->id);
-    ++done_now;
-    ++s->completed;
-  }
-  if (e != cudaSuccess) { s->err = cudaGetErrorString(e); return MSDP_ERR_CUDA; }
-  if (n_active) {
-    int a = 0;
-    for (auto* r : s->active) a += (r != nullptr);
-    *n_active = a;
-  }
+  const int rc = step_async(s, iterations, budget_s, &done_now);
+  if (rc) return rc;
+  if (n_active) *n_active = count_active(s);
   if (n_completed) *n_completed = done_now;
   return MSDP_OK;
 }
 
 int msdp_server_step(msdp_server* s, int32_t iterations, int32_t* n_active, int32_t* n_completed) {
-  return msdp_server_step_budget(s, iterations, 0.0, n_active, n_completed);
+  if (!s || iterations <= 0) return MSDP_ERR_INVALID_ARGUMENT;
+  int done_now = 0;
+  // finish every running wave first, so that the wave below covers every
+  // active request, then wait for it
+  for (auto& w : s->waves) {
+    if (!w.busy) continue;
+    cudaError_t e = cudaEventSynchronize(w.done);
+    if (e == cudaSuccess) e = harvest_wave(s, w, &done_now);
+    if (e != cudaSuccess) { s->err = cudaGetErrorString(e); return MSDP_ERR_CUDA; }
+  }
+  int rc = step_async(s, iterations, 0.0, &done_now);
+  if (rc) return rc;
+  for (auto& w : s->waves) {
+    if (!w.busy) continue;
+    cudaError_t e = cudaEventSynchronize(w.done);
+    if (e == cudaSuccess) e = harvest_wave(s, w, &done_now);
+    if (e != cudaSuccess) { s->err = cudaGetErrorString(e); return MSDP_ERR_CUDA; }
+  }
+  if (n_active) *n_active = count_active(s);
+  if (n_completed) *n_completed = done_now;
+  return MSDP_OK;
 }
 
 int msdp_server_counts(const msdp_server* s, int32_t* pending, int32_t* active, int64_t* completed) {
   if (!s) return MSDP_ERR_INVALID_ARGUMENT;
   if (pending) *pending = (int32_t)s->pending.size();
-  if (active) {
-    int a = 0;
-    for (auto* r : s->active) a += (r != nullptr);
-    *active = a;
-  }
+  if (active) *active = count_active(s);
   if (completed) *completed = s->completed;
   return MSDP_OK;
 }

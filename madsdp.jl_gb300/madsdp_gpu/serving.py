@@ -65,11 +65,18 @@ class Server:
         return rid.value
 
     def step(self, iterations: int = 2, budget_s: float = 0.0) -> Tuple[int, int]:
-        """One wave: admit, initialize newcomers, then up to `iterations`
-        iterations per active request (stopping after `budget_s` seconds
-        of the wave once each has run one, when budget_s > 0)."""
+        """budget_s = 0: one synchronous wave (admit, initialize newcomers,
+        `iterations` iterations per active request).  budget_s > 0: collect
+        finished waves and start a wave over the idle requests on a free
+        stream without waiting (waves overlap on the GPU); each request of
+        a wave runs until the wave has lasted budget_s and every request
+        of it has iterated once."""
         act, done = C.c_int32(), C.c_int32()
-        rc = self.lib.msdp_server_step_budget(self.h, int(iterations), float(budget_s), C.byref(act), C.byref(done))
+        if budget_s > 0:
+            rc = self.lib.msdp_server_step_budget(self.h, int(iterations), float(budget_s), C.byref(act),
+                                                  C.byref(done))
+        else:
+            rc = self.lib.msdp_server_step(self.h, int(iterations), C.byref(act), C.byref(done))
         if rc != 0:
             raise RuntimeError(f"msdp_server_step: {_lib.ERRORS.get(rc, rc)}")
         return act.value, done.value
@@ -114,13 +121,16 @@ class Server:
             if cnt.value < capacity:
                 return out
 
-    def drain(self, iterations: int = 2, max_steps: int = 100000, budget_s: float = 0.0) -> None:
-        """Step until nothing is pending or active."""
+    def drain(self, iterations: int = 2, max_steps: int = 1000000, budget_s: float = 0.0) -> None:
+        """Step until nothing is pending or active (with budget_s > 0 the
+        waves run asynchronously and this polls them)."""
         for _ in range(max_steps):
             p, a, _ = self.counts()
             if p == 0 and a == 0:
                 return
             self.step(iterations, budget_s)
+            if budget_s > 0:
+                time.sleep(1e-4)
         raise RuntimeError("server did not drain")
 
 
@@ -178,7 +188,10 @@ def serve_stream(server: Server, stream: Sequence[Tuple[float, str, Model]], ite
         elif nxt < len(stream):
             time.sleep(min(0.002, max(0.0, stream[nxt][0] - now)))
         t_after = time.perf_counter() - t0
-        for rid in server.finished():
+        fin = server.finished()
+        if not fin and (p or a) and budget_s > 0:
+            time.sleep(2e-4)  # waves are running; poll again shortly
+        for rid in fin:
             r = server.result(rid)
             arr, kind = ids.pop(rid)
             lat.append(t_after - arr)
