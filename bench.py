@@ -198,9 +198,17 @@ def run_instance(args):
     model = instance_model(spec, args.seed)
     ctx = M.Context(0)
     stream = torch.cuda.ExternalStream(ctx.stream_handle, device=torch.device("cuda", 0))
-    solver = M.InstanceSolver(model, context=ctx)
+    # the engine MadSDPSolver(model) picks: one thread block (a one-problem
+    # batch) for small problems, the whole-GPU solver for large ones
+    engine = "instance" if M.solver._use_instance_engine(model) else "batch"
+    if engine == "instance":
+        solver = M.InstanceSolver(model, context=ctx)
+        run = solver.solve
+    else:
+        solver = M.Batch([model], context=ctx)
+        run = solver.solve
     for _ in range(args.warmup):
-        solver.solve()
+        run()
     sampler = ClockSampler(0)
     sampler.start()
     ms, launches = [], solver.launch_count
@@ -208,19 +216,23 @@ def run_instance(args):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
-        solver.solve()
+        run()
         e1.record(stream)
         torch.cuda.synchronize()
         ms.append(e0.elapsed_time(e1))
     clocks = sampler.stop()
     launches = solver.launch_count - launches
-    st = solver.stats()
+    if engine == "instance":
+        st = solver.stats()
+        phases = {k: round(v, 4) for k, v in solver.profile().items()}
+    else:
+        st = solver.stats(0)
+        phases = None
     device_bytes = solver.device_bytes
-    phases = {k: round(v, 4) for k, v in solver.profile().items()}
     solver.close()
     # end to end: upload, solve, download through the public API
     t = time.perf_counter()
-    e2 = M.InstanceSolver(model, context=ctx)
+    e2 = M.MadSDPSolver(model, engine=engine, context=ctx)
     e2.solve()
     X, y, x, z = e2.solution()
     e2e_s = time.perf_counter() - t
@@ -248,7 +260,8 @@ def run_instance(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": args.workload, **{k: v for k, v in spec.items() if k != "kind"}, "seed": args.seed,
                    "m": model.m, "components": "PrimalDual(NT, EigenStep, Mehrotra) + DenseCholesky, ScaledIdentity",
-                   "engine": "whole-GPU instance solver (cuBLAS/cuSOLVER dense algebra + own assembly/residual kernels)",
+                   "engine": ("whole-GPU instance solver (cuBLAS/cuSOLVER dense algebra + own assembly/residual kernels)"
+                              if engine == "instance" else "one thread block (persistent batch kernel, one problem)"),
                    "status": str(st["status"]), "iterations": st["iter"], "pobj": st["pobj"], "gap": st["gap"],
                    "inf_pr": st["inf_pr"], "inf_du": st["inf_du"], "phase_seconds_last_solve": phases,
                    "l2": f"{device_bytes / 2**20:.0f} MiB resident"},

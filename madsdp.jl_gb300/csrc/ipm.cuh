@@ -473,13 +473,15 @@ struct Algo {
     bool conv;
     int sweeps = 0;
     PROF_BEGIN(j);
-    if (sizeof(T) == 8 && prm.precision == MSDP_MIXED && 2 * nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) {
+    if (sizeof(T) == 8 && prm.precision == MSDP_MIXED) {
       // FP64 phase of the mixed path: eigenvectors by FP32 Jacobi, then
       // M V and Lx V in FP64 and a few FP64 polishing sweeps (quadratic
-      // convergence from the FP32 basis).
+      // convergence from the FP32 basis).  Operands live in shared memory
+      // when they fit, else in the (idle) FP32 workspace and FP64 scratch.
       const Blk<float> bf = make_blk<float>(B, P, blk_index(b));
-      float* sMf = (float*)smem;
-      float* sVf = sMf + nn;
+      const bool smem32 = 2 * nn * (int64_t)sizeof(float) <= MSDP_SMEM_BYTES;
+      float* sMf = smem32 ? (float*)smem : bf.W(W_T1);
+      float* sVf = smem32 ? sMf + nn : bf.W(W_T2);
       for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
         sMf[k] = (float)M[k];
         sVf[k] = ((k % n) == (k / n)) ? 1.0f : 0.0f;
@@ -490,13 +492,18 @@ struct Algo {
       T* V64 = b.W(W_T2);
       for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) V64[k] = (T)sVf[k];
       __syncthreads();
-      T* sM = (T*)smem;
-      T* sB = sM + nn;
-      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, M, V64, (T)0, sM, Scratch{nullptr, 0});
-      cta_gemm<T>(n, 0, 0, 1, 0, (T)1, b.W(W_LX), V64, (T)0, sB, Scratch{nullptr, 0});
+      const bool smem64 = 2 * nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES;
+      T* sM = smem64 ? (T*)smem : b.W(W_T3);
+      T* sB = smem64 ? sM + nn : GV;
+      const Scratch gs = smem64 ? Scratch{nullptr, 0} : scr();
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, M, V64, (T)0, sM, gs);
+      cta_gemm<T>(n, 0, 0, 1, 0, (T)1, b.W(W_LX), V64, (T)0, sB, gs);
       conv = cta_jacobi_svd<T>(n, sM, sB, D, 40, &sh.counter, &sweeps);
       sweeps += 1000 * sw32;
-      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) { M[k] = sM[k]; GV[k] = sB[k]; }
+      for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+        M[k] = sM[k];
+        if (sB != GV) GV[k] = sB[k];
+      }
       __syncthreads();
     } else if (2 * nn * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) {
       T* sM = (T*)smem;
@@ -616,6 +623,14 @@ struct Algo {
       }
       return;
     }
+    if (b.structure == STRUCT_HANKEL && Lg == Rg) {
+      constexpr int PAD = 4;  // >= tile - 1: window indices leave [0, n) by at most 3
+      const int np = n + 2 * PAD;
+      if ((int64_t)np * np * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) {
+        hankel_tiled(n, Lg, H);
+        return;
+      }
+    }
     const T* L = Lg;
     const T* R = Rg;
     const int64_t need = (Lg == Rg ? 1 : 2) * nn * (int64_t)sizeof(T);
@@ -668,6 +683,73 @@ struct Algo {
       }
       H[j + (int64_t)k * m] += acc;
       if (j != k) H[k + (int64_t)j * m] += acc;
+    }
+    __syncthreads();
+  }
+
+  // Hankel 0/1 constraints with L = R = W (NT, DualCentering):
+  // H_jk = sum_a sum_c W[a,c] W[k-c, j-a], a 2-D correlation of W with
+  // itself.  W is copied into shared memory with a zero border of 4, so the
+  // index ranges need no bounds tests.  Each thread computes a 4 x 4 tile of
+  // H (lower tile triangle) and slides a 4 x 4 register window along c: per
+  // (a, c) step it loads W[a,c] and 4 new window values for 16 FMAs.
+  __noinline__ __device__ void hankel_tiled(int n, const T* W, T* H) {
+    constexpr int PAD = 4, TJ = 4, TK = 4;
+    const int m = 2 * n - 1, np = n + 2 * PAD;
+    T* Wp = (T*)smem;
+    for (int64_t q = threadIdx.x; q < (int64_t)np * np; q += NTHREADS) {
+      const int r = (int)(q % np) - PAD, c = (int)(q / np) - PAD;
+      Wp[q] = (r >= 0 && r < n && c >= 0 && c < n) ? W[r + (int64_t)c * n] : (T)0;
+    }
+    __syncthreads();
+    // Wp(r, s) = W[r, s] for r, s in [-PAD, n + PAD)
+    const T* W0 = Wp + PAD + (int64_t)PAD * np;
+    const int tiles = (m + TJ - 1) / TJ;
+    const int64_t ntp = (int64_t)tiles * (tiles + 1) / 2;
+    for (int64_t idx = threadIdx.x; idx < ntp; idx += NTHREADS) {
+      int tj, tk;
+      tri_index(idx, tj, tk);
+      const int j0 = tj * TJ, k0 = tk * TK;
+      const int a_lo = max(0, j0 - n + 1), a_hi = min(j0 + TJ - 1, n - 1);
+      const int c_lo = max(0, k0 - n + 1), c_hi = min(k0 + TK - 1, n - 1);
+      T acc[TJ][TK];
+#pragma unroll
+      for (int dj = 0; dj < TJ; ++dj)
+#pragma unroll
+        for (int dk = 0; dk < TK; ++dk) acc[dj][dk] = (T)0;
+      for (int a = a_lo; a <= a_hi; ++a) {
+        const T* Wa = W0 + a;  // W[a, c] = Wa[c * np]
+        T win[TJ][TK];         // win[dj][dk] = W[k0 + dk - c, j0 + dj - a]
+#pragma unroll
+        for (int dj = 0; dj < TJ; ++dj) {
+          const T* col = W0 + (int64_t)(j0 + dj - a) * np + k0 - c_lo;
+#pragma unroll
+          for (int dk = 0; dk < TK; ++dk) win[dj][dk] = col[dk];
+        }
+        for (int c = c_lo; c <= c_hi; ++c) {
+          const T w = Wa[(int64_t)c * np];
+#pragma unroll
+          for (int dj = 0; dj < TJ; ++dj)
+#pragma unroll
+            for (int dk = 0; dk < TK; ++dk) acc[dj][dk] = fma(w, win[dj][dk], acc[dj][dk]);
+#pragma unroll
+          for (int dj = 0; dj < TJ; ++dj) {
+#pragma unroll
+            for (int dk = TK - 1; dk > 0; --dk) win[dj][dk] = win[dj][dk - 1];
+            win[dj][0] = W0[(int64_t)(j0 + dj - a) * np + k0 - (c + 1)];
+          }
+        }
+      }
+#pragma unroll
+      for (int dj = 0; dj < TJ; ++dj)
+#pragma unroll
+        for (int dk = 0; dk < TK; ++dk) {
+          const int j = j0 + dj, k = k0 + dk;
+          if (j < m && k < m && j >= k) {
+            H[j + (int64_t)k * m] += acc[dj][dk];
+            if (j != k) H[k + (int64_t)j * m] += acc[dj][dk];
+          }
+        }
     }
     __syncthreads();
   }

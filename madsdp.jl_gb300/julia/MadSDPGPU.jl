@@ -98,7 +98,7 @@ stats (status as `MadNLP.Status`), X blocks, y, x and z.
 function solve(model::LRO.Model; direction = MadSDP.NT(), step = MadSDP.EigenStep(),
                centering = MadSDP.Mehrotra(), algorithm = MadSDP.PrimalDual(direction, step, centering),
                initial_point = MadSDP.default_initial_point(algorithm), schur = MadSDP.DenseCholesky(),
-               precision = :fp64, device = 0, options...)
+               precision = :fp64, device = 0, engine = :auto, options...)
     nb, ns, m = LRO.num_matrices(model), LRO.num_scalars(model), model.meta.ncon
     sides = Int32[LRO.side_dimension(model, LRO.MatrixIndex(i)) for i in 1:nb]
     Cs = [Matrix{Float64}(LRO.grad(model, LRO.MatrixIndex(i))) for i in 1:nb]
@@ -122,6 +122,33 @@ function solve(model::LRO.Model; direction = MadSDP.NT(), step = MadSDP.EigenSte
         comp = components(; algorithm, direction, step, centering, initial_point, schur, precision)
         ctx = Ref{Ptr{Cvoid}}(C_NULL)
         check(C_NULL, ccall((:msdp_context_create, LIB), Cint, (Cint, Ptr{Ptr{Cvoid}}), device, ctx), "context")
+        if engine == :instance || (engine == :auto && (maximum(sides; init = 0) > 160 || m > 600))
+            # one large problem on the whole GPU (msdp_solver_*)
+            sv = Ref{Ptr{Cvoid}}(C_NULL)
+            rc = ccall((:msdp_solver_create, LIB), Cint,
+                       (Ptr{Cvoid}, Ref{ProblemDesc}, Ref{Components}, Ref{Options}, Ptr{Ptr{Cvoid}}),
+                       ctx[], desc, comp, o, sv)
+            check(ctx[], rc, "msdp_solver_create")
+            if initial_point isa MadSDP.InitialPoint
+                Xs = [Matrix{Float64}(X) for X in initial_point.X]
+                check(ctx[], ccall((:msdp_solver_set_initial_point, LIB), Cint,
+                                   (Ptr{Cvoid}, Ptr{Ptr{Float64}}, Ptr{Float64}, Ptr{Float64}),
+                                   sv[], [pointer(X) for X in Xs], initial_point.y,
+                                   isnothing(initial_point.x) ? C_NULL : Vector{Float64}(initial_point.x)),
+                      "initial point")
+            end
+            check(ctx[], ccall((:msdp_solver_solve, LIB), Cint, (Ptr{Cvoid},), sv[]), "msdp_solver_solve")
+            st = Ref{Stats}()
+            check(ctx[], ccall((:msdp_solver_get_stats, LIB), Cint, (Ptr{Cvoid}, Ptr{Stats}), sv[], st), "stats")
+            X = [zeros(n, n) for n in sides]
+            y, x, z = zeros(m), zeros(ns), zeros(ns)
+            check(ctx[], ccall((:msdp_solver_get_solution, LIB), Cint,
+                               (Ptr{Cvoid}, Ptr{Ptr{Float64}}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                               sv[], [pointer(Xi) for Xi in X], y, x, z), "solution")
+            ccall((:msdp_solver_destroy, LIB), Cint, (Ptr{Cvoid},), sv[])
+            ccall((:msdp_context_destroy, LIB), Cint, (Ptr{Cvoid},), ctx[])
+            return (stats = st[], status = MadNLP.Status(st[].status), X = X, y = y, x = x, z = z)
+        end
         batch = Ref{Ptr{Cvoid}}(C_NULL)
         rc = ccall((:msdp_batch_create, LIB), Cint,
                    (Ptr{Cvoid}, Ref{ProblemDesc}, Int32, Ref{Components}, Ref{Options}, Ptr{Ptr{Cvoid}}),

@@ -498,6 +498,12 @@ class MadSDPSolver:
         self.instance = InstanceSolver(model, **kwargs) if engine == "instance" else None
         self._stats = None
 
+    def close(self):
+        """Release the device memory of the underlying batch or solver."""
+        for h in (self.batch, self.instance):
+            if h is not None:
+                h.close()
+
     def initialize(self):
         if self.batch is None:
             raise NotImplementedError("the whole-GPU engine solves in one call")

@@ -206,6 +206,20 @@ def test_mixed_late_fp32_steps_stay_interior(gpu_ctx):
         assert max(s["inf_pr"], s["inf_du"], s["gap"]) <= 1e-7
 
 
+def test_mixed_blocks_beyond_shared_memory(gpu_ctx):
+    """Blocks whose FP64 Jacobi operands exceed shared memory (n > 67) polish
+    the FP32 eigenvectors through global scratch."""
+    models = [g.sos_hankel(79, seed=31), g.maxcut(100, 0.04, seed=32), g.sos_hankel(120, seed=33)]
+    bt = M.Batch(models, precision="mixed")
+    bt.solve()
+    for m, st in zip(models, bt.all_stats()):
+        ref = o.Solver(m).solve()
+        assert st["status"] == M.Status.SOLVE_SUCCEEDED, st
+        assert max(st["inf_pr"], st["inf_du"], st["gap"]) <= 1e-7
+        scale = max(1.0, abs(ref.primal_objective()) + abs(ref.dual_objective()))
+        assert abs(st["pobj"] - ref.primal_objective()) <= 5e-7 * scale
+
+
 def test_batch_uneven_results_independent_of_mix(gpu_ctx):
     """A problem's result is the same alone and inside an uneven batch."""
     models = [g.sos_hankel(7, seed=5), g.maxcut(30, 0.2, seed=3), g.sos_hankel(20, seed=6),
