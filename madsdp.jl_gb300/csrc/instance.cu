@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "../../include/madsdp_gpu.h"
+#include "la.cuh"
 
 struct msdp_context;
 extern "C" void* msdp_context_stream(const msdp_context* ctx);
@@ -249,6 +250,47 @@ __global__ void k_aff_lin(int ns, double a, double b, const double* x, const dou
     out[i] = (x[i] + a * dx[i]) * (z[i] + b * dz[i]);
 }
 
+// svec of m symmetric n x n matrices (column-major upper triangle,
+// off-diagonal entries times sqrt 2): <B_j, B_k> = svec(B_j) . svec(B_k)
+__global__ void k_svec_pack(int n, int m, const double* __restrict__ Bm, double* __restrict__ Sv) {
+  const int64_t K = (int64_t)n * (n + 1) / 2, N = K * m;
+  const double r2 = 1.4142135623730951;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < N; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = idx / K, t = idx % K;
+    int64_t q = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (q * (q + 1) / 2 > t) --q;
+    while ((q + 1) * (q + 2) / 2 <= t) ++q;
+    const int64_t pr = t - q * (q + 1) / 2;
+    const double v = Bm[pr + q * n + j * (int64_t)n * n];
+    Sv[idx] = pr == q ? v : r2 * v;
+  }
+}
+
+// lambda_min of formed symmetric matrices Z (n <= 128), one warp per
+// matrix: Lanczos with full reorthogonalization and Sturm bisection of the
+// tridiagonal (the routine of the per-problem kernel), basis in global
+// memory.  All eigenproblems of one step-length evaluation run in one launch.
+struct LanczosJob {
+  int n;
+  const double* Z;
+  double* Q;   // n x n basis
+  double* ws;  // 4 (n + 1)
+  double* out;
+};
+
+__global__ void k_lanczos_batched(const LanczosJob* __restrict__ jobs) {
+  const LanczosJob j = jobs[blockIdx.x];
+  if (threadIdx.x < 32) {
+    double* a = j.ws;
+    double* bb = a + j.n + 1;
+    double* w = bb + j.n + 1;
+    double* coef = w + j.n + 1;
+    int steps = 0;
+    const double lam = warp_lanczos_eigmin<double>(j.n, j.Z, j.Q, 0, j.Q, a, bb, w, coef, &steps);
+    if (threadIdx.x == 0) *j.out = lam;
+  }
+}
+
 // ---- coordinate-list constraints of one block
 // out[j] (+)= sum_{e in j} v_e X[r_e, c_e]
 __global__ void k_jprod(int m, const int64_t* __restrict__ conptr, const int32_t* __restrict__ row,
@@ -334,6 +376,8 @@ struct msdp_solver {
   double* work = nullptr;
   int lwork = 0;
   double *lq = nullptr, *lh = nullptr;  // Lanczos basis (n x (kLanczosMax + 1)) and projections
+  double *lq2 = nullptr, *lw2 = nullptr;  // bases and work of the batched device Lanczos
+  void* ljobs = nullptr;
   int* dinfo = nullptr;
   double *partial = nullptr, *slots = nullptr;
   double* hslots = nullptr;
@@ -665,7 +709,10 @@ void schur_complement(S* s, double* H) {
       gemm(s, CUBLAS_OP_T, CUBLAS_OP_N, n, n * m, n, 1.0, b.G, n, b.Aall, n, 0.0, s->Tb, n);
       CB(s, cublasDgemmStridedBatched(s->cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, s->Tb, n, (long long)n * n, b.G,
                                       n, 0, &zero, s->Bb, n, (long long)n * n, m));
-      CB(s, cublasDsyrk(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, m, n * n, &one, s->Bb, n * n, &one, H, m));
+      // H += svec(B)' svec(B): K = n(n+1)/2 instead of n^2 (T is free again)
+      const int K = n * (n + 1) / 2;
+      LAUNCH(s, k_svec_pack, (int64_t)K * m, n, m, s->Bb, s->Tb);
+      CB(s, cublasDsyrk(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, m, K, &one, s->Tb, K, &one, H, m));
     } else {
       // T_k = S^-1 A_k X ; H_jk += <A_j, T_k>
       gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n * m, n, 1.0, b.Si, n, b.Aall, n, 0.0, s->Tb, n);
@@ -771,6 +818,7 @@ void correction(S* s) {
 // eigensolver).
 constexpr int kLanczosMin = 257;
 constexpr int kLanczosMax = 320;
+constexpr int kLanczosWarpMax = 128;  // batched one-warp device Lanczos up to this size
 
 // number of eigenvalues of the tridiagonal (a, b) below x (Sturm count)
 int sturm_count(const std::vector<double>& a, const std::vector<double>& b, int k, double x) {
@@ -882,25 +930,31 @@ bool lanczos_eigmin(S* s, int n, const double* Z, double* out) {
 
 // ---- step lengths (src/step.jl:148-228)
 // slot of lambda_min(L^-1 D L^-T) (src/step.jl:150-163)
-int eigmin_congruence(S* s, Blk& b, const double* L, const double* D) {
-  const int n = b.n;
+// Z = sym(L^-1 D L^-T) into Z (src/step.jl:150-163)
+void form_congruence(S* s, int n, const double* L, const double* D, double* Z) {
   const double one = 1.0;
-  CU(s, cudaMemcpyAsync(b.T1, D, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, s->st));
+  CU(s, cudaMemcpyAsync(Z, D, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, s->st));
   CB(s, cublasDtrsm(s->cb, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one, L, n,
-                    b.T1, n));
+                    Z, n));
   CB(s, cublasDtrsm(s->cb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, n, &one, L,
-                    n, b.T1, n));
-  LAUNCH(s, k_sym, (int64_t)n * n, n, b.T1);
+                    n, Z, n));
+  LAUNCH(s, k_sym, (int64_t)n * n, n, Z);
+}
+
+// slot of lambda_min(Z) for n > kLanczosWarpMax: host-driven Lanczos from
+// kLanczosMin on, else (or when it does not converge) the dense eigensolver
+int eigmin_large(S* s, Blk& b, double* Z) {
+  const int n = b.n;
   if (n >= kLanczosMin) {
     double lam = 0.0;
-    if (lanczos_eigmin(s, n, b.T1, &lam)) {
+    if (lanczos_eigmin(s, n, Z, &lam)) {
       const int slot = s->nslot++;
       CU(s, cudaMemcpyAsync(s->slots + slot, &lam, sizeof(double), cudaMemcpyHostToDevice, s->st));
       return slot;
     }
   }
   const int k = next_info(s);
-  CS(s, cusolverDnDsyevd(s->cs, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_LOWER, n, b.T1, n, b.w, s->work, s->lwork,
+  CS(s, cusolverDnDsyevd(s->cs, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_LOWER, n, Z, n, b.w, s->work, s->lwork,
                          s->dinfo + k));
   return copy_slot(s, b.w);
 }
@@ -944,9 +998,30 @@ bool step_lengths(S* s, double* a_out, double* b_out) {
     return backtrack(s, true, a_out) && backtrack(s, false, b_out);
   reset_slots(s);
   std::vector<int> lx, ls;
+  std::vector<LanczosJob> jobs;
+  int64_t qoff = 0, woff = 0;
   for (auto& b : s->B) {
-    lx.push_back(eigmin_congruence(s, b, b.Lx, b.dX));
-    ls.push_back(eigmin_congruence(s, b, b.Ls, b.dS));
+    const int n = b.n;
+    // Z_X = Lx^-1 dX Lx^-T in T1, Z_S = Ls^-1 dS Ls^-T in T2
+    form_congruence(s, n, b.Lx, b.dX, b.T1);
+    form_congruence(s, n, b.Ls, b.dS, b.T2);
+    if (n <= kLanczosWarpMax) {
+      for (int side = 0; side < 2; ++side) {
+        const int slot = s->nslot++;
+        jobs.push_back(LanczosJob{n, side ? b.T2 : b.T1, s->lq2 + qoff, s->lw2 + woff, s->slots + slot});
+        qoff += (int64_t)n * n;
+        woff += 4 * (int64_t)(n + 1);
+        (side ? ls : lx).push_back(slot);
+      }
+    } else {
+      lx.push_back(eigmin_large(s, b, b.T1));
+      ls.push_back(eigmin_large(s, b, b.T2));
+    }
+  }
+  if (!jobs.empty()) {
+    CU(s, cudaMemcpyAsync(s->ljobs, jobs.data(), sizeof(LanczosJob) * jobs.size(), cudaMemcpyHostToDevice, s->st));
+    k_lanczos_batched<<<(unsigned)jobs.size(), 32, 0, s->st>>>((const LanczosJob*)s->ljobs);
+    s->launches += 1;
   }
   const int rx = s->ns ? reduce(s, RED_MINRATIO, s->ns, s->x, s->dx) : -1;
   const int rz = s->ns ? reduce(s, RED_MINRATIO, s->ns, s->z, s->dz) : -1;
@@ -1339,6 +1414,18 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
     s->lq = vec((int64_t)nmax * (kLanczosMax + 1));
     s->lh = vec(kLanczosMax + 1);
     if (!s->lq || !s->lh) return bail(MSDP_ERR_OUT_OF_MEMORY);
+  }
+  {
+    // batched device Lanczos: two bases (X and S side) per small block
+    int64_t q = 0, w = 0, nj = 0;
+    for (auto& b : s->B)
+      if (b.n <= kLanczosWarpMax) { q += 2 * (int64_t)b.n * b.n; w += 8 * (int64_t)(b.n + 1); nj += 2; }
+    if (nj) {
+      s->lq2 = vec(q);
+      s->lw2 = vec(w);
+      s->ljobs = dalloc<unsigned char>(s, (int64_t)sizeof(LanczosJob) * nj);
+      if (!s->lq2 || !s->lw2 || !s->ljobs) return bail(MSDP_ERR_OUT_OF_MEMORY);
+    }
   }
   double bn = 0.0, dn = 0.0;
   for (int j = 0; j < m; ++j) bn = std::max(bn, std::fabs(d->b[j]));

@@ -16,7 +16,10 @@
 #include "layout.h"
 
 #ifndef MSDP_SMEM_BYTES
-#define MSDP_SMEM_BYTES (72 * 1024)
+#ifndef MSDP_SMEM_KB
+#define MSDP_SMEM_KB 72
+#endif
+#define MSDP_SMEM_BYTES (MSDP_SMEM_KB * 1024)
 #endif
 
 // Device code of one translation unit: internal linkage.
@@ -625,9 +628,13 @@ struct Algo {
     }
     if (b.structure == STRUCT_HANKEL && Lg == Rg) {
       constexpr int PAD = 4;  // >= tile - 1: window indices leave [0, n) by at most 3
-      const int np = n + 2 * PAD;
-      if ((int64_t)np * np * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES) {
-        hankel_tiled(n, Lg, H);
+      const int64_t np = n + 2 * PAD;
+      // the padded copy of W: shared memory, else the three consecutive
+      // n x n scratch matrices T1..T3 of the block (free during assembly)
+      T* Wp = np * np * (int64_t)sizeof(T) <= MSDP_SMEM_BYTES ? (T*)smem
+              : (np * np <= 3 * nn ? b.W(W_T1) : nullptr);
+      if (Wp) {
+        hankel_tiled(n, Lg, H, Wp);
         return;
       }
     }
@@ -689,14 +696,13 @@ struct Algo {
 
   // Hankel 0/1 constraints with L = R = W (NT, DualCentering):
   // H_jk = sum_a sum_c W[a,c] W[k-c, j-a], a 2-D correlation of W with
-  // itself.  W is copied into shared memory with a zero border of 4, so the
-  // index ranges need no bounds tests.  Each thread computes a 4 x 4 tile of
+  // itself.  W is copied into Wp (shared memory, or global scratch for large
+  // n) with a zero border of 4, so the index ranges need no bounds tests.  Each thread computes a 4 x 4 tile of
   // H (lower tile triangle) and slides a 4 x 4 register window along c: per
   // (a, c) step it loads W[a,c] and 4 new window values for 16 FMAs.
-  __noinline__ __device__ void hankel_tiled(int n, const T* W, T* H) {
+  __noinline__ __device__ void hankel_tiled(int n, const T* W, T* H, T* Wp) {
     constexpr int PAD = 4, TJ = 4, TK = 4;
     const int m = 2 * n - 1, np = n + 2 * PAD;
-    T* Wp = (T*)smem;
     for (int64_t q = threadIdx.x; q < (int64_t)np * np; q += NTHREADS) {
       const int r = (int)(q % np) - PAD, c = (int)(q / np) - PAD;
       Wp[q] = (r >= 0 && r < n && c >= 0 && c < n) ? W[r + (int64_t)c * n] : (T)0;

@@ -289,7 +289,10 @@ __device__ void run_op(const BatchDev& B, Prob& P, unsigned char* smem, SharedSt
 }
 
 template <int MIXED>
-__global__ void __launch_bounds__(NTHREADS, 3) msdp_ipm_kernel(const __grid_constant__ BatchDev B) {
+#ifndef MSDP_MIN_CTAS
+#define MSDP_MIN_CTAS 3
+#endif
+__global__ void __launch_bounds__(NTHREADS, MSDP_MIN_CTAS) msdp_ipm_kernel(const __grid_constant__ BatchDev B) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ SharedState sh;
   if (threadIdx.x == 0) sh.t0 = globaltimer_ns();

@@ -7,7 +7,10 @@
 #include "la.cuh"
 
 #ifndef MSDP_SMEM_BYTES
-#define MSDP_SMEM_BYTES (72 * 1024)
+#ifndef MSDP_SMEM_KB
+#define MSDP_SMEM_KB 72
+#endif
+#define MSDP_SMEM_BYTES (MSDP_SMEM_KB * 1024)
 #endif
 
 // mixed = 0: FP64 kernel; mixed = 1: FP32 phase + FP64 phase kernel

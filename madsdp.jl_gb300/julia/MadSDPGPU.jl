@@ -122,7 +122,7 @@ function solve(model::LRO.Model; direction = MadSDP.NT(), step = MadSDP.EigenSte
         comp = components(; algorithm, direction, step, centering, initial_point, schur, precision)
         ctx = Ref{Ptr{Cvoid}}(C_NULL)
         check(C_NULL, ccall((:msdp_context_create, LIB), Cint, (Cint, Ptr{Ptr{Cvoid}}), device, ctx), "context")
-        if engine == :instance || (engine == :auto && (maximum(sides; init = 0) > 160 || m > 600))
+        if engine == :instance || (engine == :auto && (maximum(sides; init = 0) > 64 || m > 300))
             # one large problem on the whole GPU (msdp_solver_*)
             sv = Ref{Ptr{Cvoid}}(C_NULL)
             rc = ccall((:msdp_solver_create, LIB), Cint,

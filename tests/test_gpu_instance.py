@@ -124,3 +124,35 @@ def test_auto_engine_and_unsupported(gpu_ctx):
         M.InstanceSolver(g.maxcut(30, 0.2, seed=1), schur=M.QRSchur())
     with pytest.raises(NotImplementedError):
         M.InstanceSolver(g.maxcut(30, 0.2, seed=1), precision="mixed")
+
+
+# ---------------------------------------------------------------- full sizes
+def test_config2_maxcut_n2000_matches_oracle(gpu_ctx):
+    """MaxCut n = 2000, p = 0.005, weights +-1 (configuration 2) at full
+    size: same iteration count, objectives and per-iteration trajectory as
+    the oracle."""
+    model = g.maxcut(2000, 0.005, weights="pm1", seed=4)
+    s = inst(model)
+    ref = o.Solver(model).solve()
+    assert_matches_oracle(s, ref)
+
+
+def test_config3_dense_mixed_cones_full_size(gpu_ctx):
+    """Blocks [200, 100, 50, 50] + 500 scalars, m = 2000, dense A
+    (configuration 3) at full size, where the oracle does not finish one
+    iteration in a minute: size-independent checks instead.  NT and HKM
+    both reach 1e-7, their objectives agree, and the dual is feasible by
+    construction of the instance (y0 gives S0 = I)."""
+    model = g.dense_random([200, 100, 50, 50], 500, 2000, seed=4)
+    nt = inst(model)
+    hkm = inst(model, direction=M.HKM())
+    for s in (nt, hkm):
+        assert s.status == M.Status.SOLVE_SUCCEEDED, s.stats
+        assert max(s.inf_pr, s.inf_du, s.inf_compl) <= 1e-7
+    scale = max(1.0, abs(nt.primal_objective()) + abs(nt.dual_objective()))
+    assert abs(nt.primal_objective() - hkm.primal_objective()) <= 1e-6 * scale
+    assert abs(nt.dual_objective() - hkm.dual_objective()) <= 1e-6 * scale
+    X, y, x, z = nt.solution()
+    for Xi in X:
+        assert np.linalg.eigvalsh((Xi + Xi.T) / 2)[0] > -1e-8
+    assert np.all(x > -1e-10) and np.all(z > -1e-10)

@@ -23,7 +23,7 @@ def comps(spec, mod):
 
 
 def gpu_solve(model, **kw):
-    return M.MadSDPSolver(model, **kw).solve()
+    return M.MadSDPSolver(model, engine="batch", **kw).solve()
 
 
 @pytest.mark.parametrize("case", [c for c in KA["cases"] if "objective" in c], ids=lambda c: c["name"])
