@@ -200,9 +200,9 @@ def run_instance(args):
     stream = torch.cuda.ExternalStream(ctx.stream_handle, device=torch.device("cuda", 0))
     # the engine MadSDPSolver(model) picks: one thread block (a one-problem
     # batch) for small problems, the whole-GPU solver for large ones
-    engine = "instance" if M.solver._use_instance_engine(model) else "batch"
+    engine = "instance" if (args.precision == "fp64_tensor" or M.solver._use_instance_engine(model)) else "batch"
     if engine == "instance":
-        solver = M.InstanceSolver(model, context=ctx)
+        solver = M.InstanceSolver(model, context=ctx, precision=args.precision)
         run = solver.solve
     else:
         solver = M.Batch([model], context=ctx)
@@ -232,7 +232,7 @@ def run_instance(args):
     solver.close()
     # end to end: upload, solve, download through the public API
     t = time.perf_counter()
-    e2 = M.MadSDPSolver(model, engine=engine, context=ctx)
+    e2 = M.MadSDPSolver(model, engine=engine, context=ctx, precision=args.precision)
     e2.solve()
     X, y, x, z = e2.solution()
     e2e_s = time.perf_counter() - t
@@ -257,8 +257,9 @@ def run_instance(args):
     line = {
         "metric": METRIC, "value": 1.0 / t_solve, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(ms), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, **{k: v for k, v in spec.items() if k != "kind"}, "seed": args.seed,
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64 (tensor-core emulated products)",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "precision": args.precision, **{k: v for k, v in spec.items() if k != "kind"}, "seed": args.seed,
                    "m": model.m, "components": "PrimalDual(NT, EigenStep, Mehrotra) + DenseCholesky, ScaledIdentity",
                    "engine": ("whole-GPU instance solver (cuBLAS/cuSOLVER dense algebra + own assembly/residual kernels)"
                               if engine == "instance" else "one thread block (persistent batch kernel, one problem)"),
@@ -569,6 +570,8 @@ def main():
     ap.add_argument("--serve-iterations", type=int, default=1000)
     ap.add_argument("--serve-budget-ms", type=float, default=20.0)
     ap.add_argument("--workload", default="sos_batch", choices=["sos_batch", *INSTANCE_WORKLOADS])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_tensor"],
+                    help="instance workloads: FP64, or FP64 products emulated on tensor cores")
     args = ap.parse_args()
     if args.workload != "sos_batch":
         if args.impl == "reference":

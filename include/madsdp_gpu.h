@@ -43,7 +43,9 @@ enum msdp_step_length { MSDP_EIGEN_STEP = 0, MSDP_CHOLESKY_BACKTRACK = 1 };
 enum msdp_centering { MSDP_MEHROTRA = 0, MSDP_ADAPTIVE_MU = 1 };
 enum msdp_initial_point { MSDP_SCALED_IDENTITY = 0, MSDP_INITIAL_POINT = 1, MSDP_DUAL_SHIFT = 2 };
 enum msdp_schur_solver { MSDP_DENSE_CHOLESKY = 0, MSDP_MADNLP_SCHUR = 1, MSDP_QR_SCHUR = 2 };
-enum msdp_precision { MSDP_FP64 = 0, MSDP_MIXED = 1 };
+/* MSDP_FP64_TENSOR: whole-GPU solver only; its dense double-precision
+ * products run as cuBLAS's fixed-point FP64 emulation on tensor cores. */
+enum msdp_precision { MSDP_FP64 = 0, MSDP_MIXED = 1, MSDP_FP64_TENSOR = 2 };
 
 /* ---- statuses (MadNLP.Status values used by MadSDP, src/moi.jl:16-29) --- */
 enum msdp_status {

@@ -185,6 +185,8 @@ int msdp_batch_create(msdp_context* ctx, const msdp_problem_desc* probs, int32_t
   }
   if (c.schur == MSDP_QR_SCHUR && c.precision != MSDP_FP64)
     return fail(ctx, MSDP_ERR_INVALID_ARGUMENT, "QRSchur requires Float64 data.");
+  if (c.precision != MSDP_FP64 && c.precision != MSDP_MIXED)
+    return fail(ctx, MSDP_ERR_UNSUPPORTED, "this precision runs on the whole-GPU solver only");
 
   if (c.initial_point == MSDP_SCALED_IDENTITY && c.scale != 0.0 && !(std::isfinite(c.scale) && c.scale > 0.0))
     return fail(ctx, MSDP_ERR_INVALID_ARGUMENT, "The identity scale must be finite and positive.");

@@ -1265,7 +1265,8 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   if (comp) c = *comp; else msdp_default_components(&c);
   if (opt) o = *opt; else msdp_default_options(&o);
   if (d->nblocks < 0 || d->m < 0 || d->ns < 0 || (d->nblocks == 0 && d->ns == 0)) return MSDP_ERR_INVALID_ARGUMENT;
-  if (c.algorithm != MSDP_PRIMAL_DUAL || c.schur != MSDP_DENSE_CHOLESKY || c.precision != MSDP_FP64)
+  if (c.algorithm != MSDP_PRIMAL_DUAL || c.schur != MSDP_DENSE_CHOLESKY ||
+      (c.precision != MSDP_FP64 && c.precision != MSDP_FP64_TENSOR))
     return MSDP_ERR_UNSUPPORTED;
   if (!(c.tau > 0.0) || !(c.shrink > 0.0 && c.shrink < 1.0) || !(c.boundary > 0.0 && c.boundary <= 1.0) ||
       o.max_iter < 0 || (c.initial_point == MSDP_DUAL_SHIFT && !(c.initial_shift > 0.0)))
@@ -1289,6 +1290,13 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
     return bail(MSDP_ERR_CUDA);
   cublasSetStream(s->cb, s->st);
   cusolverDnSetStream(s->cs, s->st);
+  if (c.precision == MSDP_FP64_TENSOR) {
+    // double-precision products by fixed-point emulation on tensor cores
+    // (cuBLAS picks the mantissa width for FP64 accuracy)
+    if (cublasSetMathMode(s->cb, CUBLAS_FP64_EMULATED_FIXEDPOINT_MATH) != CUBLAS_STATUS_SUCCESS ||
+        cublasSetEmulationStrategy(s->cb, CUBLAS_EMULATION_STRATEGY_EAGER) != CUBLAS_STATUS_SUCCESS)
+      return bail(MSDP_ERR_UNSUPPORTED);
+  }
   for (auto& e : s->ev)
     if (cudaEventCreate(&e) != cudaSuccess) e = nullptr;
   // ---- host staging of the constraints

@@ -626,6 +626,18 @@ struct Algo {
       }
       return;
     }
+    if constexpr (sizeof(T) == 8) {
+      // float64 Hankel blocks from n = 32 on: FFT along the column index;
+      // the scratch is the eight consecutive n x n matrices T1 .. ERD of the
+      // block, free during assembly ((2n-1)(N/2+1) complex <= 8 n^2 doubles)
+      int N = 1;
+      while (N < 2 * n - 1) N <<= 1;
+      const bool fits = (int64_t)(N / 2 + NWARPS * N) * 16 <= MSDP_SMEM_BYTES;  // twiddles + warp buffers
+      if (b.structure == STRUCT_HANKEL && Lg == Rg && n >= 32 && fits) {
+        hankel_fft(n, Lg, H, b.W(W_T1));
+        return;
+      }
+    }
     if (b.structure == STRUCT_HANKEL && Lg == Rg) {
       constexpr int PAD = 4;  // >= tile - 1: window indices leave [0, n) by at most 3
       const int64_t np = n + 2 * PAD;
@@ -756,6 +768,109 @@ struct Algo {
             if (j != k) H[k + (int64_t)j * m] += acc[dj][dk];
           }
         }
+    }
+    __syncthreads();
+  }
+
+  // Hankel 0/1 constraints with L = R = W in float64 for larger blocks:
+  // H(j, k) = sum_{a+b=j} (row_a * row_b)(k), the linear convolution of
+  // rows of W.  Rows are transformed by a length-N FFT along the column
+  // index (N = power of two >= 2n-1, so circular = linear convolution);
+  // per frequency w, Hh(j, w) = sum_{a+b=j} F_a(w) F_b(w) (n^2 complex
+  // multiply-adds); an inverse FFT per j gives H(j, :).  O(n^3) instead of
+  // the O(n^4) of the direct sum.  Only w <= N/2 is stored (real rows give
+  // Hermitian spectra).  S: (2n-1) (N/2+1) complex scratch, column w at
+  // S + w (2n-1).
+  __device__ static void warp_fft(int N, int logN, double2* buf, const double2* tw, bool inverse) {
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < N; i += 32) {
+      const int r = (int)(__brev((unsigned)i) >> (32 - logN));
+      if (i < r) {
+        const double2 t = buf[i];
+        buf[i] = buf[r];
+        buf[r] = t;
+      }
+    }
+    __syncwarp();
+    for (int len = 2; len <= N; len <<= 1) {
+      const int half = len >> 1, step = N / len;
+      for (int q = lane; q < N / 2; q += 32) {
+        const int pos = q % half;
+        const int i = (q / half) * len + pos, i2 = i + half;
+        double2 w = tw[pos * step];
+        if (inverse) w.y = -w.y;
+        const double2 u = buf[i], v0 = buf[i2];
+        const double2 v = make_double2(v0.x * w.x - v0.y * w.y, v0.x * w.y + v0.y * w.x);
+        buf[i] = make_double2(u.x + v.x, u.y + v.y);
+        buf[i2] = make_double2(u.x - v.x, u.y - v.y);
+      }
+      __syncwarp();
+    }
+  }
+
+  __noinline__ __device__ void hankel_fft(int n, const double* W, double* H, double* S) {
+    // S: interleaved (re, im) doubles; the workspace is only 8-byte aligned
+    const int m = 2 * n - 1;
+    int N = 1, logN = 0;
+    while (N < m) { N <<= 1; ++logN; }
+    const int Nh = N / 2 + 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double2* tw = (double2*)smem;                      // N/2 twiddles e^{-2 pi i t / N}
+    double2* buf = tw + N / 2 + (int64_t)warp * N;     // per-warp FFT buffer
+    for (int t = threadIdx.x; t < N / 2; t += NTHREADS) {
+      double sn, cs;
+      sincospi(2.0 * (double)t / (double)N, &sn, &cs);
+      tw[t] = make_double2(cs, -sn);
+    }
+    __syncthreads();
+    // forward transforms of the rows
+    for (int a = warp; a < n; a += NWARPS) {
+      for (int c = lane; c < N; c += 32) buf[c] = make_double2(c < n ? W[a + (int64_t)c * n] : 0.0, 0.0);
+      __syncwarp();
+      warp_fft(N, logN, buf, tw, false);
+      for (int w = lane; w < Nh; w += 32) {
+        double* e = S + 2 * ((int64_t)w * m + a);
+        e[0] = buf[w].x;
+        e[1] = buf[w].y;
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    // per frequency: convolution over the row index (in place per column)
+    for (int w = warp; w < Nh; w += NWARPS) {
+      double* col = S + 2 * (int64_t)w * m;
+      for (int a = lane; a < n; a += 32) buf[a] = make_double2(col[2 * a], col[2 * a + 1]);
+      __syncwarp();
+      for (int j = lane; j < m; j += 32) {
+        const int a0 = max(0, j - n + 1), a1 = min(j, n - 1);
+        double re = 0.0, im = 0.0;
+        for (int a = a0; a <= a1; ++a) {
+          const double2 f = buf[a], g2 = buf[j - a];
+          re = fma(f.x, g2.x, fma(-f.y, g2.y, re));
+          im = fma(f.x, g2.y, fma(f.y, g2.x, im));
+        }
+        col[2 * j] = re;
+        col[2 * j + 1] = im;
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    // inverse transforms per j (Hermitian completion), real part / N
+    const double invN = 1.0 / (double)N;
+    for (int j = warp; j < m; j += NWARPS) {
+      for (int w = lane; w < N; w += 32) {
+        if (w < Nh) {
+          const double* e = S + 2 * ((int64_t)w * m + j);
+          buf[w] = make_double2(e[0], e[1]);
+        } else {
+          const double* e = S + 2 * ((int64_t)(N - w) * m + j);
+          buf[w] = make_double2(e[0], -e[1]);
+        }
+      }
+      __syncwarp();
+      warp_fft(N, logN, buf, tw, true);
+      for (int k = lane; k < m; k += 32) H[j + (int64_t)k * m] += buf[k].x * invN;
+      __syncwarp();
     }
     __syncthreads();
   }

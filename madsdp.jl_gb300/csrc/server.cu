@@ -483,6 +483,7 @@ int msdp_server_create(msdp_context* ctx, const msdp_components* comp, const msd
   msdp_options o;
   if (comp) c = *comp; else msdp_default_components(&c);
   if (opt) o = *opt; else msdp_default_options(&o);
+  if (c.precision != MSDP_FP64 && c.precision != MSDP_MIXED) return MSDP_ERR_UNSUPPORTED;
   if (c.algorithm == MSDP_DUAL_CENTERING || (c.schur == MSDP_QR_SCHUR && c.precision != MSDP_FP64) ||
       (c.schur == MSDP_QR_SCHUR && c.direction != MSDP_NT) || !(c.shrink > 0.0 && c.shrink < 1.0) ||
       !(c.boundary > 0.0 && c.boundary <= 1.0) || !(c.tau > 0.0) || o.max_iter < 0 ||

@@ -69,7 +69,7 @@ function components(; algorithm, direction, step, centering, initial_point, schu
     ir, r = centering isa MadSDP.AdaptiveMu ? (Float64(centering.initial_ratio), Float64(centering.ratio)) : (x.initial_ratio, x.ratio)
     scale = initial_point isa MadSDP.ScaledIdentity && !isnothing(initial_point.scale) ? Float64(initial_point.scale) : 0.0
     ish, msh = initial_point isa MadSDP.DualShift ? (Float64(initial_point.initial_shift), Float64(initial_point.max_shift)) : (x.initial_shift, x.max_shift)
-    return Components(alg, dir, stp, cen, ip, sch, precision === :mixed ? Int32(1) : Int32(0),
+    return Components(alg, dir, stp, cen, ip, sch, precision === :mixed ? Int32(1) : precision === :fp64_tensor ? Int32(2) : Int32(0),
                       x.centering_max_iter, tau, shrink, boundary, sexp, ir, r, scale, ish, msh,
                       x.dc_beta, x.dc_delta, x.dc_A)
 end
@@ -122,7 +122,7 @@ function solve(model::LRO.Model; direction = MadSDP.NT(), step = MadSDP.EigenSte
         comp = components(; algorithm, direction, step, centering, initial_point, schur, precision)
         ctx = Ref{Ptr{Cvoid}}(C_NULL)
         check(C_NULL, ccall((:msdp_context_create, LIB), Cint, (Cint, Ptr{Ptr{Cvoid}}), device, ctx), "context")
-        if engine == :instance || (engine == :auto && (maximum(sides; init = 0) > 64 || m > 300))
+        if engine == :instance || precision === :fp64_tensor || (engine == :auto && (maximum(sides; init = 0) > 64 || m > 300))
             # one large problem on the whole GPU (msdp_solver_*)
             sv = Ref{Ptr{Cvoid}}(C_NULL)
             rc = ccall((:msdp_solver_create, LIB), Cint,

@@ -172,4 +172,5 @@ class Options:
     mixed_refine: int = 2
 
 
-PRECISIONS = {"fp64": 0, "mixed": 1}
+# "fp64_tensor": whole-GPU solver, FP64 products emulated on tensor cores
+PRECISIONS = {"fp64": 0, "mixed": 1, "fp64_tensor": 2}

@@ -497,10 +497,11 @@ class MadSDPSolver:
         if engine == "auto":
             # the whole-GPU engine runs PrimalDual + DenseCholesky in FP64
             schur = kwargs.get("schur")
+            prec = kwargs.get("precision", "fp64")
             supported = (not isinstance(kwargs.get("algorithm"), DualCentering)
                          and (schur is None or isinstance(schur, DenseCholesky))
-                         and kwargs.get("precision", "fp64") == "fp64")
-            engine = "instance" if supported and _use_instance_engine(model) else "batch"
+                         and prec in ("fp64", "fp64_tensor"))
+            engine = "instance" if supported and (prec == "fp64_tensor" or _use_instance_engine(model)) else "batch"
         self.engine = engine
         self.batch = Batch([model], **kwargs) if engine == "batch" else None
         self.instance = InstanceSolver(model, **kwargs) if engine == "instance" else None

@@ -117,6 +117,18 @@ def test_initial_points(gpu_ctx):
     assert_matches_oracle(s, ref)
 
 
+@pytest.mark.parametrize("model_name", ["maxcut400", "dense"])
+def test_fp64_tensor_emulation_matches_oracle(gpu_ctx, model_name):
+    """precision="fp64_tensor": the dense double-precision products run as
+    fixed-point FP64 emulation on tensor cores; the trajectory still matches
+    the FP64 oracle at the FP64 tolerances."""
+    model = g.maxcut(400, 0.02, weights="pm1", seed=3) if model_name == "maxcut400" else \
+        g.dense_random([14, 9], 6, 40, seed=5)
+    s = M.MadSDPSolver(model, precision="fp64_tensor").solve()
+    assert s.engine == "instance"
+    assert_matches_oracle(s, o.Solver(model).solve())
+
+
 def test_auto_engine_and_unsupported(gpu_ctx):
     assert M.MadSDPSolver(g.maxcut(200, 0.05, seed=1)).engine == "instance"
     assert M.MadSDPSolver(g.maxcut(30, 0.2, seed=1)).engine == "batch"
@@ -124,6 +136,8 @@ def test_auto_engine_and_unsupported(gpu_ctx):
         M.InstanceSolver(g.maxcut(30, 0.2, seed=1), schur=M.QRSchur())
     with pytest.raises(NotImplementedError):
         M.InstanceSolver(g.maxcut(30, 0.2, seed=1), precision="mixed")
+    with pytest.raises(NotImplementedError):
+        M.Batch([g.maxcut(30, 0.2, seed=1)], precision="fp64_tensor")
 
 
 # ---------------------------------------------------------------- full sizes

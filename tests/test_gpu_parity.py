@@ -175,6 +175,21 @@ def test_sos_batch_fp64(gpu_ctx, direction):
         compare_trajectories(bt.trajectory(i), ref.trajectory)
 
 
+def test_sos_batch_fft_assembly(gpu_ctx):
+    """Gram blocks of 32 and more assemble the Hankel Schur matrix in float64
+    through an FFT along one index; trajectories still match the oracle."""
+    models = sos_batch(n=6, seed=7, dmin=31, dmax=90)
+    bt = M.Batch(models)
+    bt.solve()
+    for i, (m, st) in enumerate(zip(models, bt.all_stats())):
+        ref = o.Solver(m).solve()
+        assert st["status"] == M.Status.SOLVE_SUCCEEDED, (i, st)
+        scale = max(1.0, abs(ref.primal_objective()) + abs(ref.dual_objective()))
+        assert abs(st["pobj"] - ref.primal_objective()) <= 1e-7 * scale
+        assert abs(st["iter"] - ref.iter) <= 1
+        compare_trajectories(bt.trajectory(i), ref.trajectory)
+
+
 def test_sos_batch_mixed(gpu_ctx):
     """Mixed precision reaches the same tolerance; its error against the
     FP64 oracle is within the tolerance of the objective gap."""
