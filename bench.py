@@ -184,6 +184,33 @@ def cpu_instance_sample(spec, seed, seconds):
     return (statistics.mean(iters) if iters else None), len(iters), init
 
 
+def run_instance_reference(args):
+    """The oracle on the same large instance, all BLAS threads: a bounded
+    number of iterations, solve time = init + mean iteration x iterations to
+    1e-7 (the iteration count of the oracle's own run when it finishes, else
+    of the GPU run recorded by the same workload)."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    spec = INSTANCE_WORKLOADS[args.workload]
+    per_it, nit, init = cpu_instance_sample(spec, args.seed, args.cpu_seconds)
+    iters = {"maxcut_n100": 11, "maxcut_n2000": 16, "dense_mixed_cones": 18}[args.workload]
+    cores = os.cpu_count() or 1
+    line = {"impl": "reference", "metric": METRIC, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": args.workload, **{k: v for k, v in spec.items() if k != "kind"},
+                                            "seed": args.seed}}
+    if per_it is None:
+        line.update(value=None, cpu_baseline={"value": None, "unit": UNIT, "cores": cores, "kind": "port",
+                                              "sample": f"no oracle iteration finished within {args.cpu_seconds:.0f} s"})
+    else:
+        v = 1.0 / ((init or 0.0) + per_it * iters)
+        line.update(value=v, cpu_baseline={"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                           "sample": f"oracle on the same instance: {nit} iterations timed, "
+                                                     f"init + mean iteration x {iters}"})
+    line["e2e"] = {"value": line["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    print(json.dumps(line), flush=True)
+
+
 def run_instance(args):
     """One large problem per step on the whole GPU (msdp_solver)."""
     import numpy as np
@@ -575,7 +602,7 @@ def main():
     args = ap.parse_args()
     if args.workload != "sos_batch":
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the default workload"}))
+            run_instance_reference(args)
             return
         run_instance(args)
     elif args.impl == "reference":
