@@ -1087,6 +1087,57 @@ struct Algo {
   // which are congruent to Lx^-1 dX Lx^-T and Ls^-1 dS Ls^-T; HKM uses the
   // triangular inverses.  Warp 0 and warp 1 run the two Lanczos iterations
   // concurrently.
+  // Smallest eigenvalues of ZX and ZS (n <= 256) by two warps, with Z, the
+  // first basis columns and the work vectors staged in shared memory when
+  // they fit; results in sh.bc[2] (X side) and sh.bc[3] (S side).
+  template <class U>
+  __device__ void lanczos_pair(int n, const U* ZX, const U* ZS, U* QX, U* QS, U* vX, U* vS, int& steps) {
+    const int64_t nn = (int64_t)n * n;
+      // per Lanczos: Z (n^2), kq basis columns and 4 vectors in shared memory
+      const int64_t vec = 4 * (int64_t)(n + 1);
+      const int64_t cap = MSDP_SMEM_BYTES / (int64_t)sizeof(U);
+      int kq2 = (int)min((int64_t)n, max((int64_t)0, (cap / 2 - nn - vec) / n));   // two concurrent
+      int kq1 = (int)min((int64_t)n, max((int64_t)0, (cap - nn - vec) / n));       // one at a time
+      const bool concurrent = kq2 >= min(n, 16);
+      const int kq = concurrent ? kq2 : kq1;
+      const bool staged = (kq >= 1);
+      const int64_t per = nn + (int64_t)kq * n + vec;
+      U* base0 = (U*)smem;
+      U* base1 = concurrent ? base0 + per : base0;
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int pass = 0; pass < (concurrent || !staged ? 1 : 2); ++pass) {
+        // stage the Z matrices this pass needs
+        if (staged) {
+          if (concurrent || pass == 0)
+            for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) base0[k] = ZX[k];
+          if (concurrent || pass == 1)
+            for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) base1[k] = ZS[k];
+          __syncthreads();
+        }
+        const bool runx = (concurrent || !staged) ? (warp == 0) : (pass == 0 && warp == 0);
+        const bool runs = (concurrent || !staged) ? (warp == 1) : (pass == 1 && warp == 0);
+        if (runx) {
+          U* bs = base0;
+          const U* z = staged ? bs : ZX;
+          U* v = staged ? bs + nn + (int64_t)kq * n : vX;
+          const U lam = staged
+              ? warp_lanczos_eigmin<U>(n, z, bs + nn, kq, QX, v, v + (n + 1), v + 2 * (n + 1), v + 3 * (n + 1), &steps)
+              : warp_lanczos_eigmin<U>(n, z, QX, n, QX, vX, vX + (n + 1), vX + 2 * (n + 1), vX + 3 * (n + 1), &steps);
+          if (lane == 0) { sh.bc[2] = (double)lam; sh.bc[4] = (double)steps; }
+        } else if (runs) {
+          U* bs = base1;
+          const U* z = staged ? bs : ZS;
+          U* v = staged ? bs + nn + (int64_t)kq * n : vS;
+          const U lam = staged
+              ? warp_lanczos_eigmin<U>(n, z, bs + nn, kq, QS, v, v + (n + 1), v + 2 * (n + 1), v + 3 * (n + 1), &steps)
+              : warp_lanczos_eigmin<U>(n, z, QS, n, QS, vS, vS + (n + 1), vS + 2 * (n + 1), vS + 3 * (n + 1), &steps);
+          if (lane == 0) { sh.bc[3] = (double)lam; sh.bc[5] = (double)steps; }
+        }
+        __syncthreads();
+      }
+      steps = (int)(sh.bc[4] + sh.bc[5]);
+  }
+
   __noinline__ __device__ void eigen_steps(const Blk<T>& b, double tau, double& ax, double& as) {
     const int n = b.n;
     const int64_t nn = b.nn;
@@ -1115,50 +1166,26 @@ struct Algo {
     }
     PROF_BEGIN(l);
     int steps = 0;
-    if (n <= 256) {
-      // per Lanczos: Z (n^2), kq basis columns and 4 vectors in shared memory
-      const int64_t vec = 4 * (int64_t)(n + 1);
-      const int64_t cap = MSDP_SMEM_BYTES / (int64_t)sizeof(T);
-      int kq2 = (int)min((int64_t)n, max((int64_t)0, (cap / 2 - nn - vec) / n));   // two concurrent
-      int kq1 = (int)min((int64_t)n, max((int64_t)0, (cap - nn - vec) / n));       // one at a time
-      const bool concurrent = kq2 >= min(n, 16);
-      const int kq = concurrent ? kq2 : kq1;
-      const bool staged = (kq >= 1);
-      const int64_t per = nn + (int64_t)kq * n + vec;
-      T* base0 = (T*)smem;
-      T* base1 = concurrent ? base0 + per : base0;
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      for (int pass = 0; pass < (concurrent || !staged ? 1 : 2); ++pass) {
-        // stage the Z matrices this pass needs
-        if (staged) {
-          if (concurrent || pass == 0)
-            for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) base0[k] = ZX[k];
-          if (concurrent || pass == 1)
-            for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) base1[k] = ZS[k];
-          __syncthreads();
-        }
-        const bool runx = (concurrent || !staged) ? (warp == 0) : (pass == 0 && warp == 0);
-        const bool runs = (concurrent || !staged) ? (warp == 1) : (pass == 1 && warp == 0);
-        if (runx) {
-          T* bs = base0;
-          const T* z = staged ? bs : ZX;
-          T* v = staged ? bs + nn + (int64_t)kq * n : b.V(WV_LA);
-          const T lam = staged
-              ? warp_lanczos_eigmin<T>(n, z, bs + nn, kq, b.W(W_Q), v, v + (n + 1), v + 2 * (n + 1), v + 3 * (n + 1), &steps)
-              : warp_lanczos_eigmin<T>(n, z, b.W(W_Q), n, b.W(W_Q), b.V(WV_LA), b.V(WV_LB), b.V(WV_LW), b.V(WV_LC), &steps);
-          if (lane == 0) { sh.bc[2] = (double)lam; sh.bc[4] = (double)steps; }
-        } else if (runs) {
-          T* bs = base1;
-          const T* z = staged ? bs : ZS;
-          T* v = staged ? bs + nn + (int64_t)kq * n : b.V(WV_LA2);
-          const T lam = staged
-              ? warp_lanczos_eigmin<T>(n, z, bs + nn, kq, b.W(W_RNT), v, v + (n + 1), v + 2 * (n + 1), v + 3 * (n + 1), &steps)
-              : warp_lanczos_eigmin<T>(n, z, b.W(W_RNT), n, b.W(W_RNT), b.V(WV_LA2), b.V(WV_LB2), b.V(WV_LW2), b.V(WV_LC2), &steps);
-          if (lane == 0) { sh.bc[3] = (double)lam; sh.bc[5] = (double)steps; }
+    bool f32 = false;
+    if constexpr (sizeof(T) == 8) {
+      // FP64 phase of the mixed path: the step-length eigenvalues in FP32
+      // (the iteration's float64 positive-definiteness check guards the step)
+      f32 = prm.precision == MSDP_MIXED && n <= 256;
+      if (f32) {
+        const Blk<float> bf = make_blk<float>(B, P, blk_index(b));
+        float* zx = bf.W(W_T2);
+        float* zs = bf.W(W_T3);
+        for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+          zx[k] = (float)ZX[k];
+          zs[k] = (float)ZS[k];
         }
         __syncthreads();
+        lanczos_pair<float>(n, zx, zs, bf.W(W_Q), bf.W(W_RNT), bf.V(WV_LA), bf.V(WV_LA2), steps);
       }
-      steps = (int)(sh.bc[4] + sh.bc[5]);
+    }
+    if (f32) {
+    } else if (n <= 256) {
+      lanczos_pair<T>(n, ZX, ZS, b.W(W_Q), b.W(W_RNT), b.V(WV_LA), b.V(WV_LA2), steps);
     } else {
       const T* zx = ZX;
       const T* zs = ZS;
@@ -1424,6 +1451,7 @@ struct Algo {
       PROF_END(st, SC_T_STEP);
     }
     if (!strict && (!(fmin(a, bt) >= 0.2) || !step_keeps_interior(a, bt))) return false;
+    if (strict) shrink_to_interior(a, bt);
     PROF_BEGIN(tk);
     take_step(a, bt);
     PROF_END(tk, SC_T_TAKE);
@@ -1439,6 +1467,7 @@ struct Algo {
     double a, bt;
     step_lengths(a, bt);
     if (!strict && (!(fmin(a, bt) >= 0.2) || !step_keeps_interior(a, bt))) return false;
+    if (strict) shrink_to_interior(a, bt);
     take_step(a, bt);
     double mu = prm.ratio * total_complementarity() / fmax((double)nu(), 1.0);
     if (fmin(a, bt) < 0.5) mu *= 1.5;
@@ -1459,6 +1488,19 @@ struct Algo {
       if (!add_mul_posdef<double>(b.n, b.S, bt, b.dS, b.Shat, smem, sh)) return false;
     }
     return true;
+  }
+
+  // FP64 iterations of the mixed path take their step-length eigenvalues
+  // in FP32: the lengths are shrunk by 0.9 until X + a dX and S + b dS
+  // factor in float64 (at most 64 times).  A no-op on the FP64 path.
+  __noinline__ __device__ void shrink_to_interior(double& a, double& bt) {
+    if (sizeof(T) != 8 || prm.precision != MSDP_MIXED || prm.step != MSDP_EIGEN_STEP) return;
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      if (b.n > 256) continue;  // larger blocks keep float64 eigenvalues
+      for (int t = 0; t < 64 && !add_mul_posdef<double>(b.n, b.X, a, b.dX, b.Shat, smem, sh); ++t) a *= 0.9;
+      for (int t = 0; t < 64 && !add_mul_posdef<double>(b.n, b.S, bt, b.dS, b.Shat, smem, sh); ++t) bt *= 0.9;
+    }
   }
 
   __device__ bool iterate_pd(bool strict) {
