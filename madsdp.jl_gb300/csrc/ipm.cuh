@@ -1316,7 +1316,10 @@ struct Algo {
       // primal defect r = Rp - A(dX) - C_lin dx, so that the primal
       // equation holds to float64 accuracy for that scaling.
       directions64(mu, corrected, !corrected);
-      for (int pass = 0; pass < prm.mixed_refine; ++pass) {
+      const double bn = fmax(1.0, P.sc[SC_BNORM]);
+      double dmax = 0.0, rmax = 0.0;
+      for (int pass = 0;; ++pass) {
+        // float64 primal defect of the current direction
         for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.h[j] = P.Rp[j];
         __syncthreads();
         for (int i = 0; i < P.nblocks; ++i) {
@@ -1326,33 +1329,25 @@ struct Algo {
           jprod_add(b, P.m, b.buf, P.h);
         }
         if (P.ns > 0) clin_mv(P, P.delx, -1.0, P.h);
+        double dl = 0.0, rl = 0.0;
+        for (int j = threadIdx.x; j < P.m; j += NTHREADS) {
+          dl = fmax(dl, fabs(P.h[j]));
+          rl = fmax(rl, fabs(P.Rp[j]));
+        }
+        dmax = block_max(dl, &sh.rb);
+        rmax = block_max(rl, &sh.rb);
+        // at least one pass; stop early once the defect is far below the
+        // acceptance bound (further passes would not change the decision)
+        const double bound = fmax(0.1 * rmax / bn, 0.01 * prm.tol);
+        if (pass >= prm.mixed_refine || (pass >= 1 && dmax / bn <= 1e-3 * bound)) break;
         schur_solve(P.h);
         for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.dely[j] += P.h[j];
         __syncthreads();
         directions64(mu, corrected, false);
       }
-      // remaining float64 primal defect, relative as inf_pr (the caller
-      // rejects an FP32 direction that does not satisfy the primal equation)
-      for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.h[j] = P.Rp[j];
-      __syncthreads();
-      for (int i = 0; i < P.nblocks; ++i) {
-        Blk<T> b = blk(i);
-        for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) b.buf[k] = -b.dX[k];
-        __syncthreads();
-        jprod_add(b, P.m, b.buf, P.h);
-      }
-      if (P.ns > 0) clin_mv(P, P.delx, -1.0, P.h);
-      double dmax = 0.0, rmax = 0.0;
-      for (int j = threadIdx.x; j < P.m; j += NTHREADS) {
-        dmax = fmax(dmax, fabs(P.h[j]));
-        rmax = fmax(rmax, fabs(P.Rp[j]));
-      }
-      dmax = block_max(dmax, &sh.rb);
-      rmax = block_max(rmax, &sh.rb);
-      if (threadIdx.x == 0) {
-        const double bn = fmax(1.0, P.sc[SC_BNORM]);
-        sh.bc[7] = (dmax / bn > fmax(0.1 * rmax / bn, 0.01 * prm.tol)) ? 1.0 : 0.0;
-      }
+      // the caller rejects an FP32 direction whose remaining float64 primal
+      // defect (relative as inf_pr) exceeds the bound
+      if (threadIdx.x == 0) sh.bc[7] = (dmax / bn > fmax(0.1 * rmax / bn, 0.01 * prm.tol)) ? 1.0 : 0.0;
       __syncthreads();
     } else {
       directions(mu, corrected);
