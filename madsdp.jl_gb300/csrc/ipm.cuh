@@ -546,13 +546,13 @@ struct Algo {
     __syncthreads();
     // Gi = ((M V) D^-3/2)' Ls'
     cta_gemm<T>(n, 1, 1, 0, 1, (T)1, M, b.W(W_LS), (T)0, b.W(W_GI), scr());
-    cta_gemm<T>(n, 0, 1, 0, 0, (T)1, G, G, (T)0, b.W(W_W), scr());
-    cta_symmetrize<T>(n, b.W(W_W));
+    cta_gemm<T>(n, 0, 1, 0, 0, (T)1, G, G, (T)0, b.W(W_W), scr(), 1);
+    cta_lower_to_full<T>(n, b.W(W_W));
     // S^-1 = G D^-1 G'
     for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) t2[k] = G[k] / D[k / n];
     __syncthreads();
-    cta_gemm<T>(n, 0, 1, 0, 0, (T)1, t2, G, (T)0, b.W(W_SI), scr());
-    cta_symmetrize<T>(n, b.W(W_SI));
+    cta_gemm<T>(n, 0, 1, 0, 0, (T)1, t2, G, (T)0, b.W(W_SI), scr(), 1);
+    cta_lower_to_full<T>(n, b.W(W_SI));
     PROF_END(np, SC_T_NTPROD);
     return true;
   }
@@ -956,13 +956,15 @@ struct Algo {
     const int n = b.n;
     T* tmp = b.W(W_T3);
     if (is_nt()) {
+      // W M W is symmetric: the second product only for the lower triangle
       cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_W), Min, (T)0, tmp, scr());
-      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, tmp, b.W(W_W), (T)0, out, scr());
+      cta_gemm<T>(n, 0, 0, 0, 0, (T)1, tmp, b.W(W_W), (T)0, out, scr(), 1);
+      cta_lower_to_full<T>(n, out);
     } else {
       cta_gemm<T>(n, 0, 0, 0, 0, (T)1, xt(b), Min, (T)0, tmp, scr());
       cta_gemm<T>(n, 0, 0, 0, 0, (T)1, tmp, b.W(W_SI), (T)0, out, scr());
+      cta_symmetrize<T>(n, out);
     }
-    cta_symmetrize<T>(n, out);
   }
 
   // ---------------- rhs! (src/step.jl:63-89)
@@ -1059,13 +1061,15 @@ struct Algo {
           RNT[k] = -(t3[k] + t3[q + (int64_t)p * n]) / (D[p] + D[q]);
         }
         __syncthreads();
+        // G RNT G' with RNT symmetric: lower triangle only
         cta_gemm<T>(n, 0, 0, 0, 0, (T)1, b.W(W_G), RNT, (T)0, t1, scr());
-        cta_gemm<T>(n, 0, 1, 0, 0, (T)1, t1, b.W(W_G), (T)0, corr, scr());
+        cta_gemm<T>(n, 0, 1, 0, 0, (T)1, t1, b.W(W_G), (T)0, corr, scr(), 1);
+        cta_lower_to_full<T>(n, corr);
       } else {
         cta_gemm<T>(n, 0, 0, 0, 0, (T)1, dxt, dst, (T)0, t1, scr());
         cta_gemm<T>(n, 0, 0, 0, 0, (T)-1, t1, b.W(W_SI), (T)0, corr, scr());
+        cta_symmetrize<T>(n, corr);
       }
-      cta_symmetrize<T>(n, corr);
     }
     for (int k = threadIdx.x; k < P.ns; k += NTHREADS) P.corrlin[k] = -P.delx[k] * P.delz[k] * P.zinv[k];
     __syncthreads();
@@ -1379,8 +1383,9 @@ struct Algo {
         __syncthreads();
         if (rdnz) {
           cta_gemm<double>(n, 0, 0, 0, 0, 1.0, L64, b.Rd, 0.0, tmp, scr());
-          cta_gemm<double>(n, 0, 0, 0, 0, 1.0, tmp, R64, 0.0, erd, scr());
-          cta_symmetrize<double>(n, erd);
+          cta_gemm<double>(n, 0, 0, 0, 0, 1.0, tmp, R64, 0.0, erd, scr(), is_nt() ? 1 : 0);
+          if (is_nt()) cta_lower_to_full<double>(n, erd);
+          else cta_symmetrize<double>(n, erd);
         }
       }
       jtprod_combine(b, P.dely, 1.0, nullptr, nullptr, b.ATy);
@@ -1388,8 +1393,9 @@ struct Algo {
       __syncthreads();
       cta_symmetrize<double>(n, b.dS);
       cta_gemm<double>(n, 0, 0, 0, 0, 1.0, L64, b.ATy, 0.0, tmp, scr());
-      cta_gemm<double>(n, 0, 0, 0, 0, 1.0, tmp, R64, 0.0, e1, scr());
-      cta_symmetrize<double>(n, e1);
+      cta_gemm<double>(n, 0, 0, 0, 0, 1.0, tmp, R64, 0.0, e1, scr(), is_nt() ? 1 : 0);
+      if (is_nt()) cta_lower_to_full<double>(n, e1);
+      else cta_symmetrize<double>(n, e1);
       const T* Si = b.W(W_SI);
       const T* corr = b.W(W_CORR);
       for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) {

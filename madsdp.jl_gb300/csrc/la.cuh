@@ -100,6 +100,15 @@ template <class T> __device__ void cta_symmetrize(int n, T* A) {
   }
   __syncthreads();
 }
+// Upper triangle := lower triangle (after a lower-only symmetric product).
+template <class T> __device__ void cta_lower_to_full(int n, T* A) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
+    const int i = (int)(k % n), j = (int)(k / n);
+    if (i < j) A[k] = A[j + (int64_t)i * n];
+  }
+  __syncthreads();
+}
 // dst = sym(src) into another buffer.
 template <class T, class U> __device__ void cta_sym_copy(int n, T* dst, const U* src) {
   const int64_t nn = (int64_t)n * n;
@@ -122,11 +131,12 @@ template <class T> __device__ void cta_set_identity(int n, T* A, T diag) {
 // alias A or B.  Each thread owns R x R output micro-tiles.
 template <class T, int R>
 __device__ void cta_gemm_r(int n, int ta, int tb, int loA, int loB, T alpha, const T* __restrict__ A,
-                           const T* __restrict__ B, T beta, T* __restrict__ C) {
+                           const T* __restrict__ B, T beta, T* __restrict__ C, int loC = 0) {
   const int nb = (n + R - 1) / R;
   const int tiles = nb * nb;
   for (int t = threadIdx.x; t < tiles; t += NTHREADS) {
     const int i0 = (t % nb) * R, j0 = (t / nb) * R;
+    if (loC && j0 > i0 + R - 1) continue;  // only tiles touching the lower triangle
     int klo = 0, khi = n;  // k in [klo, khi)
     if (loA) {
       if (!ta) khi = min(khi, i0 + R);  // A(i,k) != 0 -> k <= i
@@ -174,9 +184,9 @@ __device__ void cta_gemm_r(int n, int ta, int tb, int loA, int loB, T alpha, con
 
 template <class T>
 __device__ __forceinline__ void cta_gemm_plain(int n, int ta, int tb, int loA, int loB, T alpha, const T* A,
-                                               const T* B, T beta, T* C) {
-  if (n <= 24) cta_gemm_r<T, 2>(n, ta, tb, loA, loB, alpha, A, B, beta, C);
-  else cta_gemm_r<T, 4>(n, ta, tb, loA, loB, alpha, A, B, beta, C);
+                                               const T* B, T beta, T* C, int loC = 0) {
+  if (n <= 24) cta_gemm_r<T, 2>(n, ta, tb, loA, loB, alpha, A, B, beta, C, loC);
+  else cta_gemm_r<T, 4>(n, ta, tb, loA, loB, alpha, A, B, beta, C, loC);
 }
 
 // Shared-memory scratch handed to the routines that stage operands
@@ -188,9 +198,11 @@ struct Scratch {
 
 // GEMM whose operands are first copied into shared memory when they fit
 // (operands written earlier by this CTA would otherwise be re-read from L2).
+// loC = 1: only the lower triangle of C is needed (a symmetric product);
+// tiles strictly above the diagonal are skipped.
 template <class T>
 __device__ void cta_gemm(int n, int ta, int tb, int loA, int loB, T alpha, const T* A, const T* B, T beta, T* C,
-                         Scratch sc) {
+                         Scratch sc, int loC = 0) {
   const int64_t nn = (int64_t)n * n;
   const int64_t need = (A == B ? 1 : 2) * nn * (int64_t)sizeof(T);
   if (sc.p != nullptr && need <= sc.bytes) {
@@ -201,9 +213,9 @@ __device__ void cta_gemm(int n, int ta, int tb, int loA, int loB, T alpha, const
       if (A != B) sB[k] = B[k];
     }
     __syncthreads();
-    cta_gemm_plain<T>(n, ta, tb, loA, loB, alpha, sA, sB, beta, C);
+    cta_gemm_plain<T>(n, ta, tb, loA, loB, alpha, sA, sB, beta, C, loC);
   } else {
-    cta_gemm_plain<T>(n, ta, tb, loA, loB, alpha, A, B, beta, C);
+    cta_gemm_plain<T>(n, ta, tb, loA, loB, alpha, A, B, beta, C, loC);
   }
 }
 
