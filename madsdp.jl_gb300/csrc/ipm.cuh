@@ -476,22 +476,32 @@ struct Algo {
     bool conv;
     int sweeps = 0;
     PROF_BEGIN(j);
-    if (sizeof(T) == 8 && prm.precision == MSDP_MIXED) {
-      // FP64 phase of the mixed path: eigenvectors by FP32 Jacobi, then
-      // M V and Lx V in FP64 and a few FP64 polishing sweeps (quadratic
-      // convergence from the FP32 basis).  Operands live in shared memory
-      // when they fit, else in the (idle) FP32 workspace and FP64 scratch.
-      const Blk<float> bf = make_blk<float>(B, P, blk_index(b));
-      const bool smem32 = 2 * nn * (int64_t)sizeof(float) <= MSDP_SMEM_BYTES;
-      float* sMf = smem32 ? (float*)smem : bf.W(W_T1);
-      float* sVf = smem32 ? sMf + nn : bf.W(W_T2);
+    const bool f32ws = prm.precision == MSDP_MIXED;  // an FP32 workspace exists
+    const bool smem32 = (2 * nn + n) * (int64_t)sizeof(float) <= MSDP_SMEM_BYTES;
+    if (sizeof(T) == 8 && (f32ws || smem32)) {
+      // float64 NT scaling (the FP64 path and the FP64 phase of the mixed
+      // path): eigenvectors by FP32 Jacobi, then M V and Lx V in FP64 and
+      // FP64 polishing sweeps to float64 convergence (quadratic from the
+      // FP32 basis).  Operands live in shared memory when they fit, else in
+      // the (idle) FP32 workspace of a mixed batch and FP64 scratch.
+      float *sMf, *sVf, *Df;
+      if (smem32) {
+        sMf = (float*)smem;
+        sVf = sMf + nn;
+        Df = sVf + nn;
+      } else {
+        const Blk<float> bf = make_blk<float>(B, P, blk_index(b));
+        sMf = bf.W(W_T1);
+        sVf = bf.W(W_T2);
+        Df = bf.V(WV_D);
+      }
       for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) {
         sMf[k] = (float)M[k];
         sVf[k] = ((k % n) == (k / n)) ? 1.0f : 0.0f;
       }
       __syncthreads();
       int sw32 = 0;
-      cta_jacobi_svd<float>(n, sMf, sVf, bf.V(WV_D), 40, &sh.counter, &sw32);
+      cta_jacobi_svd<float>(n, sMf, sVf, Df, 40, &sh.counter, &sw32);
       T* V64 = b.W(W_T2);
       for (int64_t k = threadIdx.x; k < nn; k += NTHREADS) V64[k] = (T)sVf[k];
       __syncthreads();
