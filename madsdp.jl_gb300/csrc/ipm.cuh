@@ -31,6 +31,8 @@ struct SharedState {
   int counter;
   int prob;
   int stop;
+  int erd64;     // FP32 phase: E(Rd) in float64 formed for this iteration
+  int pad2;
   double bc[8];  // broadcast scalars
   uint64_t t0;   // launch start on this CTA (globaltimer)
 };
@@ -1329,27 +1331,27 @@ struct Algo {
       // scaling, then `mixed_refine` passes of Schur solves on the float64
       // primal defect r = Rp - A(dX) - C_lin dx, so that the primal
       // equation holds to float64 accuracy for that scaling.
-      directions64(mu, corrected, !corrected);
       const double bn = fmax(1.0, P.sc[SC_BNORM]);
       double dmax = 0.0, rmax = 0.0;
-      for (int pass = 0;; ++pass) {
-        // float64 primal defect of the current direction
-        for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.h[j] = P.Rp[j];
+      if (!corrected && threadIdx.x == 0) sh.erd64 = 0;
+      __syncthreads();
+      // the FP32 direction as is, when its float64 primal defect is already
+      // far below the acceptance bound (large residuals early in the solve)
+      directions(mu, corrected);
+      primal_defect(dmax, rmax);
+      if (dmax / bn <= 1e-3 * fmax(0.1 * rmax / bn, 0.01 * prm.tol)) {
+        if (threadIdx.x == 0) sh.bc[7] = 0.0;
         __syncthreads();
-        for (int i = 0; i < P.nblocks; ++i) {
-          Blk<T> b = blk(i);
-          for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) b.buf[k] = -b.dX[k];
-          __syncthreads();
-          jprod_add(b, P.m, b.buf, P.h);
-        }
-        if (P.ns > 0) clin_mv(P, P.delx, -1.0, P.h);
-        double dl = 0.0, rl = 0.0;
-        for (int j = threadIdx.x; j < P.m; j += NTHREADS) {
-          dl = fmax(dl, fabs(P.h[j]));
-          rl = fmax(rl, fabs(P.Rp[j]));
-        }
-        dmax = block_max(dl, &sh.rb);
-        rmax = block_max(rl, &sh.rb);
+        PROF_END(d, SC_T_DIRECTIONS);
+        return;
+      }
+      const bool fresh = sh.erd64 == 0;
+      __syncthreads();
+      directions64(mu, corrected, fresh);
+      if (fresh && threadIdx.x == 0) sh.erd64 = 1;
+      __syncthreads();
+      for (int pass = 0;; ++pass) {
+        primal_defect(dmax, rmax);
         // at least one pass; stop early once the defect is far below the
         // acceptance bound (further passes would not change the decision)
         const double bound = fmax(0.1 * rmax / bn, 0.01 * prm.tol);
@@ -1370,6 +1372,26 @@ struct Algo {
     }
     PROF_END(d, SC_T_DIRECTIONS);
   }
+  // P.h = Rp - A(dX) - C_lin dx in float64; its max norm and that of Rp
+  __device__ void primal_defect(double& dmax, double& rmax) {
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) P.h[j] = P.Rp[j];
+    __syncthreads();
+    for (int i = 0; i < P.nblocks; ++i) {
+      Blk<T> b = blk(i);
+      for (int64_t k = threadIdx.x; k < b.nn; k += NTHREADS) b.buf[k] = -b.dX[k];
+      __syncthreads();
+      jprod_add(b, P.m, b.buf, P.h);
+    }
+    if (P.ns > 0) clin_mv(P, P.delx, -1.0, P.h);
+    double dl = 0.0, rl = 0.0;
+    for (int j = threadIdx.x; j < P.m; j += NTHREADS) {
+      dl = fmax(dl, fabs(P.h[j]));
+      rl = fmax(rl, fabs(P.Rp[j]));
+    }
+    dmax = block_max(dl, &sh.rb);
+    rmax = block_max(rl, &sh.rb);
+  }
+
   // whether the last solve_directions left a primal defect above its bound
   __device__ __forceinline__ bool inexact_direction() const { return sh.bc[7] != 0.0; }
 
