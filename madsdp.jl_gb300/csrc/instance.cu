@@ -1280,7 +1280,6 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   s->ns = d->ns;
   s->nb = d->nblocks;
   const int m = d->m, ns = d->ns;
-  int rc = MSDP_OK;
   auto bail = [&](int code) {
     release(s);
     delete s;
@@ -1443,7 +1442,6 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   if (ns) CU(s, cudaMemcpy(s->dlin, d->d_lin, 8 * ns, cudaMemcpyHostToDevice));
   if (ns && m) CU(s, cudaMemcpy(s->Clin, d->C_lin, 8 * (int64_t)m * ns, cudaMemcpyHostToDevice));
   if (s->fail) return bail(s->fail);
-  (void)rc;
   *out = s;
   return MSDP_OK;
 }

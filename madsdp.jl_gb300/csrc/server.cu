@@ -21,8 +21,7 @@
 #include "../../include/madsdp_gpu.h"
 #include "launch.h"
 
-struct msdp_context;  // defined in capi.cu; only its stream and error are used here
-extern "C" void* msdp_context_stream(const msdp_context* ctx);
+struct msdp_context;  // defined in capi.cu; a server runs on its own streams
 
 namespace {
 
