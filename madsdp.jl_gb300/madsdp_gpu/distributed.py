@@ -13,8 +13,6 @@ from __future__ import annotations
 import heapq
 from typing import Callable, List, Sequence
 
-import numpy as np
-
 __all__ = ["solve_cost", "shard_by_cost", "max_over_ranks", "gather_to_root", "solve_sharded"]
 
 

@@ -18,9 +18,8 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 from . import _lib
-from .components import (AdaptiveMu, CholeskyBacktrack, DenseCholesky, DualCentering, DualShift,
-                         EigenStep, HKM, InitialPoint, MadNLPSchur, Mehrotra, NT, Options,
-                         PRECISIONS, PrimalDual, QRSchur, ScaledIdentity, Status)
+from .components import (DenseCholesky, DualCentering, DualShift, EigenStep, InitialPoint, Mehrotra, NT,
+                         Options, PRECISIONS, PrimalDual, QRSchur, ScaledIdentity, Status)
 from .model import Model
 
 __all__ = ["Context", "Batch", "MadSDPSolver", "madsdp", "GPUError", "default_context"]

@@ -40,8 +40,8 @@ from __future__ import annotations
 import enum
 import math
 import time
-from dataclasses import dataclass, field
-from typing import List, Optional
+from dataclasses import dataclass
+from typing import Optional
 
 import numpy as np
 import scipy.linalg as sla
