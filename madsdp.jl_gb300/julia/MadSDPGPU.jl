@@ -106,11 +106,14 @@ function solve(model::LRO.Model; direction = MadSDP.NT(), step = MadSDP.EigenSte
     b = Vector{Float64}(LRO.cons_constant(model))
     d = Vector{Float64}(model.d_lin)
     Cl = Matrix{Float64}(model.C_lin)
-    GC.@preserve sides Cs coords b d Cl begin
-        desc = ProblemDesc(nb, m, ns, 0, pointer(sides),
-                           pointer([pointer(c) for c in Cs]), pointer(Int64[length(c[4]) for c in coords]),
-                           pointer([pointer(c[1]) for c in coords]), pointer([pointer(c[2]) for c in coords]),
-                           pointer([pointer(c[3]) for c in coords]), pointer([pointer(c[4]) for c in coords]),
+    # the pointer arrays are named so that GC.@preserve keeps them alive
+    Cp = [pointer(c) for c in Cs]
+    nnz = Int64[length(c[4]) for c in coords]
+    conp, rowp = [pointer(c[1]) for c in coords], [pointer(c[2]) for c in coords]
+    colp, valp = [pointer(c[3]) for c in coords], [pointer(c[4]) for c in coords]
+    GC.@preserve sides Cs coords b d Cl Cp nnz conp rowp colp valp begin
+        desc = ProblemDesc(nb, m, ns, 0, pointer(sides), pointer(Cp), pointer(nnz),
+                           pointer(conp), pointer(rowp), pointer(colp), pointer(valp),
                            pointer(b), pointer(d), pointer(Cl))
         opt = Ref{Options}()
         ccall((:msdp_default_options, LIB), Cvoid, (Ptr{Options},), opt)
@@ -131,10 +134,11 @@ function solve(model::LRO.Model; direction = MadSDP.NT(), step = MadSDP.EigenSte
             check(ctx[], rc, "msdp_solver_create")
             if initial_point isa MadSDP.InitialPoint
                 Xs = [Matrix{Float64}(X) for X in initial_point.X]
-                check(ctx[], ccall((:msdp_solver_set_initial_point, LIB), Cint,
+                y0 = Vector{Float64}(initial_point.y)
+                x0 = isnothing(initial_point.x) ? nothing : Vector{Float64}(initial_point.x)
+                GC.@preserve Xs y0 x0 check(ctx[], ccall((:msdp_solver_set_initial_point, LIB), Cint,
                                    (Ptr{Cvoid}, Ptr{Ptr{Float64}}, Ptr{Float64}, Ptr{Float64}),
-                                   sv[], [pointer(X) for X in Xs], initial_point.y,
-                                   isnothing(initial_point.x) ? C_NULL : Vector{Float64}(initial_point.x)),
+                                   sv[], [pointer(X) for X in Xs], y0, isnothing(x0) ? C_NULL : pointer(x0)),
                       "initial point")
             end
             check(ctx[], ccall((:msdp_solver_solve, LIB), Cint, (Ptr{Cvoid},), sv[]), "msdp_solver_solve")
@@ -156,10 +160,12 @@ function solve(model::LRO.Model; direction = MadSDP.NT(), step = MadSDP.EigenSte
         check(ctx[], rc, "msdp_batch_create")
         if initial_point isa MadSDP.InitialPoint
             Xs = [Matrix{Float64}(X) for X in initial_point.X]
-            check(ctx[], ccall((:msdp_batch_set_initial_point, LIB), Cint,
+            y0 = Vector{Float64}(initial_point.y)
+            x0 = isnothing(initial_point.x) ? nothing : Vector{Float64}(initial_point.x)
+            GC.@preserve Xs y0 x0 check(ctx[], ccall((:msdp_batch_set_initial_point, LIB), Cint,
                                (Ptr{Cvoid}, Int32, Ptr{Ptr{Float64}}, Ptr{Float64}, Ptr{Float64}),
-                               batch[], 0, [pointer(X) for X in Xs], initial_point.y,
-                               isnothing(initial_point.x) ? C_NULL : Vector{Float64}(initial_point.x)), "initial point")
+                               batch[], 0, [pointer(X) for X in Xs], y0, isnothing(x0) ? C_NULL : pointer(x0)),
+                  "initial point")
         end
         check(ctx[], ccall((:msdp_batch_solve, LIB), Cint, (Ptr{Cvoid},), batch[]), "msdp_batch_solve")
         st = Ref{Stats}()
