@@ -1,0 +1,39 @@
+"""The reference arm of bench.py (the oracle on the host cores) prints one
+JSON line with the contract's keys; runs on CPU."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def run_bench(*args):
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", *args],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    return json.loads(lines[0])
+
+
+def check_common(d):
+    assert d["impl"] == "reference"
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_batched_sos():
+    d = run_bench("--steps", "1", "--warmup", "1", "--cpu-seconds", "4", "--instances", "64")
+    check_common(d)
+    assert d["value"] > 0 and d["e2e"]["value"] == d["value"]
+    assert d["config"]["workload"] == "sos_hankel_batch"
+
+
+def test_reference_arm_single_instance():
+    d = run_bench("--workload", "maxcut_n100", "--cpu-seconds", "3")
+    check_common(d)
+    assert d["value"] > 0 and d["config"]["workload"] == "maxcut_n100"
