@@ -62,57 +62,43 @@ def flops_per_iteration(n: int, m: int, nnz: int) -> float:
     return 28.0 * n ** 3 + 2.0 * nnz * nnz / 2.0 + m ** 3 / 3.0 + 4.0 * m * m
 
 
-# ----------------------------------------------------------------- CPU oracle
-def _oracle_worker(args):
-    i, d, seed = args
-    os.environ.setdefault("OMP_NUM_THREADS", "1")
-    sys.path[:0] = [ROOT, PKG]
-    from madsdp_gpu import generators as g
-    from oracle import madsdp_oracle as o
-    t = time.perf_counter()
-    s = o.Solver(g.sos_hankel(d, seed=seed)).solve()
-    return (i, time.perf_counter() - t, int(s.status), s.primal_objective(), s.iter)
-
-
-def _timed_oracle(pool, tasks, start, seconds, cores):
-    """Keep `cores` oracle solves in flight over tasks[start:] (cyclically)
-    for `seconds`, then let the ones in flight finish.  Returns (solves/s,
-    results, next task index)."""
-    import queue
-    q = queue.Queue()
-    n = len(tasks)
-    nxt, inflight, results = start % n, 0, []
+# ----------------------------------------------------------------- CPU baseline
+def _timed_port(prep, start, seconds, cores):
+    """Solve the prepared instances from `start` on (cyclically) with the
+    compiled CPU restatement on `cores` threads, starting new solves for
+    `seconds` and letting the ones in flight finish.  Returns (solves/s,
+    results as (index, status, pobj, iter), next index)."""
+    from oracle import cpu_ipm
+    n = len(prep)
+    nxt, results = start % n, []
     t0 = time.perf_counter()
-    for _ in range(cores):
-        pool.apply_async(_oracle_worker, (tasks[nxt],), callback=q.put, error_callback=q.put)
-        nxt, inflight = (nxt + 1) % n, inflight + 1
-    while inflight:
-        r = q.get()
-        inflight -= 1
-        if isinstance(r, BaseException):
-            raise r
-        results.append(r)
-        if time.perf_counter() - t0 < seconds:
-            pool.apply_async(_oracle_worker, (tasks[nxt],), callback=q.put, error_callback=q.put)
-            nxt, inflight = (nxt + 1) % n, inflight + 1
+    while True:
+        left = seconds - (time.perf_counter() - t0)
+        if left <= 0:
+            break
+        out = cpu_ipm.solve_many(prep, cores, left, start=nxt, count=n - nxt)
+        for k, s in enumerate(out):
+            if s is not None:
+                results.append((nxt + k, s["status"], s["pobj"], s["iter"]))
+        done = sum(s is not None for s in out)
+        nxt = (nxt + done) % n
+        if done < len(out):
+            break
     return len(results) / (time.perf_counter() - t0), results, nxt
 
 
-def _oracle_pool(cores):
-    for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
-        os.environ[k] = "1"
-    return mp.get_context("spawn").Pool(cores)
+def cpu_port_prepare(models):
+    """Build the compiled CPU restatement, marshal the instances and run one
+    small solve (all untimed)."""
+    from oracle import cpu_ipm
+    cpu_ipm.build()
+    prep = cpu_ipm.Prepared(models)
+    cpu_ipm.solve_many(prep, 1, 0.0, start=0, count=1)
+    return prep
 
 
-def cpu_oracle_sample(ds, seed, seconds, cores):
-    """Solve instances of the workload with the oracle on `cores` processes
-    (started and warmed before the clock) for about `seconds`; returns
-    (solves/s, results as (index, time, status, pobj, iter), instances)."""
-    tasks = [(i, d, seed * 100003 + i) for i, d in enumerate(ds)]
-    with _oracle_pool(cores) as pool:
-        pool.map(_oracle_worker, tasks[-cores:])  # start-up and imports, untimed
-        rate, results, _ = _timed_oracle(pool, tasks, 0, seconds, cores)
-    return rate, results, len(results)
+CPU_PORT = "compiled C++ restatement of the oracle (oracle/cpu_ipm.cpp: FP64, NT+EigenStep+Mehrotra+DenseCholesky, " \
+           "own dense kernels, no BLAS)"
 
 
 # ----------------------------------------------------------------- single large instances
@@ -397,26 +383,23 @@ def profiled_traffic():
 
 # ----------------------------------------------------------------- arms
 def run_reference(args):
-    """The oracle on all host cores (one process per core, one BLAS thread
-    each) over the workload's instances, in order; each step keeps every
-    process busy for about `cpu_seconds / (warmup + steps)` seconds and lets
-    the solves in flight finish."""
+    """The compiled CPU restatement on all host cores (one solve per thread)
+    over the workload's instances, in order; each step starts solves for
+    about `cpu_seconds / (warmup + steps)` seconds and lets the ones in
+    flight finish."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     n = args.instances
-    ds = workload(n, args.seed)[1]
-    tasks = [(i, d, args.seed * 100003 + i) for i, d in enumerate(ds)]
+    models = workload(n, args.seed)[0]
     cores = os.cpu_count() or 1
-    per_step = max(5.0, args.cpu_seconds / max(1, args.steps + args.warmup))
-    vals = []
-    with _oracle_pool(cores) as pool:
-        pool.map(_oracle_worker, tasks[-cores:])  # start-up and imports, untimed
-        nxt = 0
-        for k in range(args.warmup + args.steps):
-            rate, _, nxt = _timed_oracle(pool, tasks, nxt, per_step, cores)
-            if k >= args.warmup:
-                vals.append(rate)
+    per_step = max(2.0, args.cpu_seconds / max(1, args.steps + args.warmup))
+    prep = cpu_port_prepare(models)
+    vals, nxt = [], 0
+    for k in range(args.warmup + args.steps):
+        rate, _, nxt = _timed_port(prep, nxt, per_step, cores)
+        if k >= args.warmup:
+            vals.append(rate)
     value = statistics.mean(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
@@ -425,8 +408,8 @@ def run_reference(args):
         "config": {"workload": "sos_hankel_batch", "instances": n, "d_range": [5, 63], "m": "2d+1",
                    "components": "PrimalDual(NT, EigenStep, Mehrotra) + DenseCholesky"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"oracle (NumPy/SciPy FP64 restatement of MadSDP) on the workload's instances "
-                                   f"in order, {per_step:.0f} s per step, {cores} processes x 1 BLAS thread"},
+                         "sample": f"{CPU_PORT} on the workload's instances in order, {per_step:.0f} s per step, "
+                                   f"{cores} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -438,13 +421,14 @@ def run_gpu(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     import numpy as np
 
-    # oracle pool first (spawned before any CUDA work)
+    # CPU baseline first, on the host cores before any CUDA work
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        _, ds0 = workload(args.instances, args.seed)
         cores = os.cpu_count() or 1
-        v, res, cnt = cpu_oracle_sample(ds0, args.seed, args.cpu_seconds, cores)
-        cpu = {"value": v, "results": res, "count": cnt, "cores": cores}
+        prep = cpu_port_prepare(workload(args.instances, args.seed)[0])
+        v, res, _ = _timed_port(prep, 0, args.cpu_seconds, cores)
+        cpu = {"value": v, "results": res, "count": len(res), "cores": cores}
+        del prep
 
     import torch
     import torch.distributed as dist
@@ -560,11 +544,10 @@ def run_gpu(args):
     oracle_err = None
     if cpu is not None:
         cpu_block = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": "port",
-                     "sample": f"oracle (NumPy/SciPy FP64 restatement of MadSDP, NT+EigenStep+Mehrotra) on the first "
-                               f"{cpu['count']} of the {args.instances} instances, {args.cpu_seconds:.0f} s, "
-                               f"{cpu['cores']} processes x 1 BLAS thread"}
+                     "sample": f"{CPU_PORT}: {cpu['count']} solves of the {args.instances} instances in order "
+                               f"(from the first, cyclically), {args.cpu_seconds:.0f} s, {cpu['cores']} threads"}
         errs = []
-        for i, t, status, pobj, it in cpu["results"]:
+        for i, status, pobj, it in cpu["results"]:
             s = stm[i]
             errs.append(abs(pobj - s["pobj"]) / max(1.0, abs(s["pobj"]) + abs(s["dobj"])))
         oracle_err = max(errs) if errs else None

@@ -1,0 +1,147 @@
+"""Build and ctypes binding of the compiled CPU restatement (cpu_ipm.cpp).
+
+TEST INFRASTRUCTURE ONLY, like ``madsdp_oracle``: it times the CPU baseline
+of the batched workloads without interpreter overhead.  It restates the
+default PrimalDual path (NT, EigenStep, Mehrotra, DenseCholesky,
+ScaledIdentity) of MadSDP.jl (src/solver.jl, src/primal_dual.jl,
+src/directions.jl, src/step.jl, src/blocks.jl) following ``madsdp_oracle``
+step by step, and ``tests/test_oracle_cpp.py`` checks it against that module.
+
+    build()                         g++ -O3 into oracle/lib/libmsdp_cpu.so
+    solve(model, **options)         one solve, a dict of the stats
+    solve_many(models, threads, seconds, **options)
+    symeig(A)                       eigenvalues, eigenvectors (test hook)
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+SRC = os.path.join(HERE, "cpu_ipm.cpp")
+LIB_DIR = os.path.join(HERE, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "libmsdp_cpu.so")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the library when it is missing or older than its sources."""
+    header = os.path.join(ROOT, "include", "madsdp_gpu.h")
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(header))
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
+        return LIB_PATH
+    os.makedirs(LIB_DIR, exist_ok=True)
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    cmd = ["g++", "-O3", "-std=c++17", "-shared", "-fPIC", "-Wall", "-o", tmp, SRC, "-lpthread"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    from madsdp_gpu import _lib as G
+    build()
+    lib = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    lib.msdp_cpu_default_options.restype = None
+    lib.msdp_cpu_default_options.argtypes = [P(G.Options)]
+    lib.msdp_cpu_solve.restype = C.c_int32
+    lib.msdp_cpu_solve.argtypes = [P(G.ProblemDesc), P(G.Options), P(G.Stats)]
+    lib.msdp_cpu_solve_many.restype = C.c_int32
+    lib.msdp_cpu_solve_many.argtypes = [P(G.ProblemDesc), C.c_int32, C.c_int32, C.c_double, P(G.Options),
+                                        P(G.Stats)]
+    lib.msdp_cpu_symeig.restype = C.c_int32
+    lib.msdp_cpu_symeig.argtypes = [C.c_int32, P(C.c_double), P(C.c_double), P(C.c_double)]
+    _lib = lib
+    return lib
+
+
+def _options(lib, options):
+    from madsdp_gpu import _lib as G
+    o = G.Options()
+    lib.msdp_cpu_default_options(C.byref(o))
+    for k, v in options.items():
+        if not hasattr(o, k):
+            raise TypeError(f"unknown option {k}")
+        setattr(o, k, v)
+    return o
+
+
+def _stats(s) -> dict:
+    return {k: getattr(s, k) for k, _ in s._fields_}
+
+
+def solve(model, **options) -> dict:
+    from madsdp_gpu.solver import _Marshalled
+    lib = load()
+    mm = _Marshalled(model)
+    st = _stats_struct()
+    rc = lib.msdp_cpu_solve(C.byref(mm.desc), C.byref(_options(lib, options)), C.byref(st))
+    if rc != 0:
+        raise ValueError(f"msdp_cpu_solve returned {rc}")
+    return _stats(st)
+
+
+def _stats_struct():
+    from madsdp_gpu import _lib as G
+    return G.Stats()
+
+
+class Prepared:
+    """Marshalled problems, kept alive across timed calls of solve_many."""
+
+    def __init__(self, models: Sequence):
+        from madsdp_gpu import _lib as G
+        from madsdp_gpu.solver import _Marshalled
+        self.marsh = [_Marshalled(m) for m in models]
+        self.descs = (G.ProblemDesc * len(self.marsh))(*[mm.desc for mm in self.marsh])
+        self.stats = (G.Stats * len(self.marsh))()
+
+    def __len__(self):
+        return len(self.marsh)
+
+
+def solve_many(models, threads: int, seconds: float = 0.0, start: int = 0, count: Optional[int] = None,
+               **options) -> List[Optional[dict]]:
+    """Solve models[start:start+count] on `threads` host threads, stopping
+    new solves after `seconds` (> 0).  `models` is a sequence of models or a
+    ``Prepared``.  Returns one stats dict per problem, None for the ones not
+    started."""
+    lib = load()
+    prep = models if isinstance(models, Prepared) else Prepared(models)
+    n = len(prep) - start if count is None else count
+    if start < 0 or n < 0 or start + n > len(prep):
+        raise ValueError("range outside the prepared problems")
+    for i in range(start, start + n):
+        prep.stats[i].status = -2
+    descs = C.cast(C.byref(prep.descs, start * C.sizeof(prep.descs._type_)), C.POINTER(prep.descs._type_))
+    stats = C.cast(C.byref(prep.stats, start * C.sizeof(prep.stats._type_)), C.POINTER(prep.stats._type_))
+    lib.msdp_cpu_solve_many(descs, n, threads, seconds, C.byref(_options(lib, options)), stats)
+    out = []
+    for i in range(start, start + n):
+        s = prep.stats[i]
+        out.append(None if s.status == -2 else _stats(s))
+    return out
+
+
+def symeig(A):
+    lib = load()
+    A = np.asfortranarray(A, dtype=np.float64)
+    n = A.shape[0]
+    w = np.zeros(n)
+    V = np.zeros((n, n), order="F")
+    dp = C.POINTER(C.c_double)
+    rc = lib.msdp_cpu_symeig(n, A.ctypes.data_as(dp), w.ctypes.data_as(dp), V.ctypes.data_as(dp))
+    if rc != 0:
+        raise RuntimeError(f"msdp_cpu_symeig returned {rc}")
+    return w, V
