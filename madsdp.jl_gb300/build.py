@@ -66,7 +66,7 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {cmd[-3]}")
-    link = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lcublas", "-lcusolver"]
+    link = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lcublas", "-lcusolver", "-lpthread"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         sys.stderr.write(" ".join(link) + "\n" + r.stdout + r.stderr)

@@ -6,12 +6,15 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/madsdp_gpu.h"
 #include "launch.h"
+#include "stage.h"
 
 struct msdp_context {
   int device = 0;
@@ -276,88 +279,18 @@ int msdp_batch_create(msdp_context* ctx, const msdp_problem_desc* probs, int32_t
   }
   b->n_dd = o_dd; b->n_d64 = o64; b->n_d32 = o32; b->n_ent = o_ent; b->n_ptr = o_ptr;
 
-  // ---- host staging
-  std::vector<double> hdd(o_dd, 0.0);
-  std::vector<int32_t> herow(o_ent), hecol(o_ent), hpcon(o_ent);
-  std::vector<double> heval(o_ent), hpval(o_ent);
-  std::vector<int64_t> hptr(o_ptr, 0);
-  bi = 0;
-  for (int p = 0; p < nprob; ++p) {
-    const msdp_problem_desc& d = probs[p];
-    const ProbDesc& pd = b->hprob[p];
-    const int64_t m = d.m, ns = d.ns;
-    double* dat = hdd.data() + pd.bdat;
-    double bn = 0.0, dn = 0.0, cmax = 0.0;
-    for (int64_t j = 0; j < m; ++j) { dat[j] = d.b[j]; bn = std::max(bn, std::fabs(d.b[j])); }
-    for (int64_t k = 0; k < ns; ++k) { dat[m + k] = d.d_lin[k]; dn = std::max(dn, std::fabs(d.d_lin[k])); }
-    for (int64_t k = 0; k < m * ns; ++k) dat[m + ns + k] = d.C_lin[k];
-    for (int i = 0; i < d.nblocks; ++i, ++bi) {
-      BlockDesc& bd = b->hblk[bi];
-      const int64_t n = bd.n, nn = n * n, nnz = bd.nnz;
-      double cn = 0.0;
-      for (int64_t k = 0; k < nn; ++k) {
-        hdd[bd.cdat + k] = d.C[i][k];
-        cn = std::max(cn, std::fabs(d.C[i][k]));
-      }
-      bd.cnorm = cn;
-      cmax = std::max(cmax, cn);
-      // entries sorted by (constraint, column, row)
-      const int32_t* con = d.A_con[i];
-      const int32_t* row = d.A_row[i];
-      const int32_t* col = d.A_col[i];
-      const double* val = d.A_val[i];
-      for (int64_t e = 0; e < nnz; ++e) {
-        if (con[e] < 0 || con[e] >= m || row[e] < 0 || row[e] >= n || col[e] < 0 || col[e] >= n) {
-          msdp_batch_destroy(b);
-          return fail(ctx, MSDP_ERR_INVALID_ARGUMENT, "constraint entry out of range");
-        }
-      }
-      std::vector<int64_t> idx(nnz);
-      std::iota(idx.begin(), idx.end(), 0);
-      std::sort(idx.begin(), idx.end(), [&](int64_t a, int64_t c2) {
-        if (con[a] != con[c2]) return con[a] < con[c2];
-        if (col[a] != col[c2]) return col[a] < col[c2];
-        return row[a] < row[c2];
-      });
-      int64_t* cptr = hptr.data() + bd.conptr;
-      for (int64_t e = 0; e < nnz; ++e) {
-        const int64_t s = idx[e];
-        herow[bd.ent + e] = row[s];
-        hecol[bd.ent + e] = col[s];
-        heval[bd.ent + e] = val[s];
-        cptr[con[s] + 1] += 1;
-      }
-      for (int64_t j = 0; j < m; ++j) cptr[j + 1] += cptr[j];
-      // Hankel 0/1 structure: m = 2n-1 and constraint j holds exactly the
-      // entries (a, j-a) with value 1
-      bool hankel = (m == 2 * n - 1) && nnz == n * n;
-      for (int64_t j = 0; hankel && j < m; ++j) {
-        const int64_t lo = std::max<int64_t>(0, j - n + 1), hi = std::min<int64_t>(j, n - 1);
-        if (cptr[j + 1] - cptr[j] != hi - lo + 1) { hankel = false; break; }
-        int64_t prev_col = -1;
-        for (int64_t q = cptr[j]; q < cptr[j + 1]; ++q) {
-          const int64_t e = bd.ent + q;
-          if (herow[e] + hecol[e] != j || heval[e] != 1.0 || hecol[e] <= prev_col) { hankel = false; break; }
-          prev_col = hecol[e];
-        }
-      }
-      bd.structure = choose_structure(hankel, n, m, nnz);
-      // by position (counting sort, stable in constraint order)
-      int64_t* pptr = hptr.data() + bd.posptr;
-      for (int64_t e = 0; e < nnz; ++e) pptr[row[e] + col[e] * n + 1] += 1;
-      for (int64_t k = 0; k < nn; ++k) pptr[k + 1] += pptr[k];
-      std::vector<int64_t> fill(pptr, pptr + nn);
-      for (int64_t e = 0; e < nnz; ++e) {
-        const int64_t s = idx[e];
-        const int64_t pos = row[s] + (int64_t)col[s] * n;
-        const int64_t q = fill[pos]++;
-        hpcon[bd.ent + q] = con[s];
-        hpval[bd.ent + q] = val[s];
-      }
-    }
-    dat[m + ns + m * ns + 0] = bn;
-    dat[m + ns + m * ns + 1] = dn;
-    dat[m + ns + m * ns + 2] = cmax;
+  // ---- host staging (stage.h), on the host threads
+  std::unique_ptr<double[]> hdd(new double[std::max<int64_t>(o_dd, 1)]);
+  std::unique_ptr<int32_t[]> herow(new int32_t[std::max<int64_t>(o_ent, 1)]);
+  std::unique_ptr<int32_t[]> hecol(new int32_t[std::max<int64_t>(o_ent, 1)]);
+  std::unique_ptr<int32_t[]> hpcon(new int32_t[std::max<int64_t>(o_ent, 1)]);
+  std::unique_ptr<double[]> heval(new double[std::max<int64_t>(o_ent, 1)]);
+  std::unique_ptr<double[]> hpval(new double[std::max<int64_t>(o_ent, 1)]);
+  std::unique_ptr<int64_t[]> hptr(new int64_t[std::max<int64_t>(o_ptr, 1)]);
+  const StageBuffers sb{hdd.get(), o_dd, herow.get(), hecol.get(), heval.get(), hpcon.get(), hpval.get(), hptr.get()};
+  if (!stage_batch(probs, nprob, b->hprob.data(), b->hblk.data(), sb, (int)std::thread::hardware_concurrency())) {
+    msdp_batch_destroy(b);
+    return fail(ctx, MSDP_ERR_INVALID_ARGUMENT, "constraint entry out of range");
   }
   std::vector<int32_t> order(nprob);
   std::iota(order.begin(), order.end(), 0);
@@ -384,13 +317,13 @@ int msdp_batch_create(msdp_context* ctx, const msdp_problem_desc* probs, int32_t
   up(b->dprob, b->hprob.data(), sizeof(ProbDesc) * nprob);
   up(b->dblk, b->hblk.data(), sizeof(BlockDesc) * nblk_total);
   up(b->dorder, order.data(), sizeof(int32_t) * nprob);
-  up(b->dd, hdd.data(), sizeof(double) * o_dd);
-  up(b->erow, herow.data(), sizeof(int32_t) * o_ent);
-  up(b->ecol, hecol.data(), sizeof(int32_t) * o_ent);
-  up(b->pcon, hpcon.data(), sizeof(int32_t) * o_ent);
-  up(b->eval, heval.data(), sizeof(double) * o_ent);
-  up(b->pval, hpval.data(), sizeof(double) * o_ent);
-  up(b->ptr, hptr.data(), sizeof(int64_t) * o_ptr);
+  up(b->dd, hdd.get(), sizeof(double) * o_dd);
+  up(b->erow, herow.get(), sizeof(int32_t) * o_ent);
+  up(b->ecol, hecol.get(), sizeof(int32_t) * o_ent);
+  up(b->pcon, hpcon.get(), sizeof(int32_t) * o_ent);
+  up(b->eval, heval.get(), sizeof(double) * o_ent);
+  up(b->pval, hpval.get(), sizeof(double) * o_ent);
+  up(b->ptr, hptr.get(), sizeof(int64_t) * o_ptr);
   b->upload_bytes = (int64_t)(sizeof(ProbDesc) * nprob + sizeof(BlockDesc) * nblk_total + sizeof(int32_t) * nprob +
                               sizeof(double) * o_dd + (3 * sizeof(int32_t) + 2 * sizeof(double)) * o_ent +
                               sizeof(int64_t) * o_ptr);

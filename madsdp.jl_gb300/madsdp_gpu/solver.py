@@ -170,6 +170,92 @@ class _Marshalled:
         self.desc = d
 
 
+def _cat(parts, dtype) -> np.ndarray:
+    """One contiguous array of `dtype` (at least one element, so that its
+    address is valid) from the flattened parts, converted in the copy."""
+    if not parts:
+        return np.zeros(1, dtype=dtype)
+    out = np.concatenate([np.asarray(a).reshape(-1) for a in parts], dtype=dtype, casting="unsafe")
+    return out if out.size else np.zeros(1, dtype=dtype)
+
+
+def _offsets(sizes: np.ndarray) -> np.ndarray:
+    """Exclusive prefix sum, as uint64 element offsets."""
+    off = np.zeros(sizes.size, dtype=np.uint64)
+    if sizes.size > 1:
+        np.cumsum(sizes[:-1].astype(np.uint64), out=off[1:])
+    return off
+
+
+def _desc_dtype() -> np.dtype:
+    names = [f for f, _ in _lib.ProblemDesc._fields_]
+    formats = [np.int32 if t is C.c_int32 else np.uint64 for _, t in _lib.ProblemDesc._fields_]
+    offsets = [getattr(_lib.ProblemDesc, f).offset for f in names]
+    return np.dtype({"names": names, "formats": formats, "offsets": offsets,
+                     "itemsize": C.sizeof(_lib.ProblemDesc)})
+
+
+class _MarshalledBatch:
+    """Many problems packed into a few contiguous arrays, with the table of
+    msdp_problem_desc built as one numpy structured array (each pointer is
+    the base of a packed array plus the problem's or block's offset).  It
+    holds every buffer the descriptors point to while the C call runs."""
+
+    def __init__(self, models: Sequence[Model]):
+        n = len(models)
+        nb = np.fromiter((mm.nblocks for mm in models), dtype=np.int64, count=n)
+        ms = np.fromiter((mm.m for mm in models), dtype=np.int64, count=n)
+        ns = np.fromiter((mm.ns for mm in models), dtype=np.int64, count=n)
+        blocks = [A for mm in models for A in mm.A]
+        self.sides = _cat([np.asarray(mm.sides, dtype=np.int64) for mm in models], np.int32)
+        self.nnz = np.fromiter((A.val.size for A in blocks), dtype=np.int64, count=len(blocks))
+        self.C = _cat([np.asarray(c, dtype=np.float64).ravel(order="F") for mm in models for c in mm.C], np.float64)
+        self.con = _cat([A.con for A in blocks], np.int32)
+        self.row = _cat([A.row for A in blocks], np.int32)
+        self.col = _cat([A.col for A in blocks], np.int32)
+        self.val = _cat([A.val for A in blocks], np.float64)
+        self.b = _cat([mm.b for mm in models], np.float64)
+        self.d = _cat([mm.d_lin for mm in models], np.float64)
+        self.Cl = _cat([np.asarray(mm.C_lin, dtype=np.float64).ravel(order="F") for mm in models], np.float64)
+        if self.nnz.size == 0:
+            self.nnz = np.zeros(1, dtype=np.int64)
+
+        def base(a):
+            return np.uint64(a.ctypes.data)
+
+        sides64 = np.asarray(self.sides[:len(blocks)], dtype=np.int64)
+        coff = _offsets(sides64 * sides64)
+        eoff = _offsets(self.nnz[:len(blocks)])
+        nblk = max(len(blocks), 1)
+        self.Cp = np.zeros(nblk, dtype=np.uint64)
+        self.conp, self.rowp, self.colp, self.valp = (np.zeros(nblk, dtype=np.uint64) for _ in range(4))
+        if blocks:
+            self.Cp[:] = base(self.C) + np.uint64(8) * coff
+            self.conp[:] = base(self.con) + np.uint64(4) * eoff
+            self.rowp[:] = base(self.row) + np.uint64(4) * eoff
+            self.colp[:] = base(self.col) + np.uint64(4) * eoff
+            self.valp[:] = base(self.val) + np.uint64(8) * eoff
+        boff = _offsets(nb)
+        d = np.zeros(n, dtype=_desc_dtype())
+        d["nblocks"], d["m"], d["ns"] = nb, ms, ns
+        d["sides"] = base(self.sides) + np.uint64(4) * boff
+        d["A_nnz"] = base(self.nnz) + np.uint64(8) * boff
+        for field, arr in (("C", self.Cp), ("A_con", self.conp), ("A_row", self.rowp), ("A_col", self.colp),
+                           ("A_val", self.valp)):
+            d[field] = base(arr) + np.uint64(8) * boff
+        d["b"] = base(self.b) + np.uint64(8) * _offsets(ms)
+        d["d_lin"] = base(self.d) + np.uint64(8) * _offsets(ns)
+        d["C_lin"] = base(self.Cl) + np.uint64(8) * _offsets(ms * ns)
+        self.table = d
+        self.count = n
+
+    def descs(self, start: int = 0):
+        """Pointer to the descriptor of problem `start` (and those after it)."""
+        if not 0 <= start <= self.count:
+            raise IndexError(start)
+        return C.cast(self.table.ctypes.data + start * self.table.itemsize, P(_lib.ProblemDesc))
+
+
 class Batch:
     """Many problems resident on one GPU, solved by one persistent launch."""
 
@@ -200,16 +286,16 @@ class Batch:
                     raise RuntimeError("MadSDP: `DualCentering` does not support scalar (LP) blocks yet.")
                 if m.nblocks == 0:
                     raise RuntimeError("MadSDP: `DualCentering` needs at least one PSD block.")
-        marsh = [_Marshalled(m) for m in self.models]
-        descs = (_lib.ProblemDesc * len(marsh))(*[mm.desc for mm in marsh])
+        marsh = _MarshalledBatch(self.models)
         comp = _components(self.algorithm, self.initial_point, self.schur, precision)
         opts = _options(self.opt)
         h = C.c_void_p()
-        rc = self.lib.msdp_batch_create(self.ctx.h, descs, len(marsh), C.byref(comp), C.byref(opts), C.byref(h))
+        rc = self.lib.msdp_batch_create(self.ctx.h, marsh.descs(), marsh.count, C.byref(comp), C.byref(opts),
+                                        C.byref(h))
         self.ctx.check(rc, "msdp_batch_create")
         self.h = h
         self.ctx.adopt(self)
-        self.nprob = len(marsh)
+        self.nprob = marsh.count
         if isinstance(self.initial_point, InitialPoint):
             for p in range(self.nprob):
                 self.set_initial_point(p, self.initial_point)

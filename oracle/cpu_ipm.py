@@ -102,13 +102,12 @@ class Prepared:
 
     def __init__(self, models: Sequence):
         from madsdp_gpu import _lib as G
-        from madsdp_gpu.solver import _Marshalled
-        self.marsh = [_Marshalled(m) for m in models]
-        self.descs = (G.ProblemDesc * len(self.marsh))(*[mm.desc for mm in self.marsh])
-        self.stats = (G.Stats * len(self.marsh))()
+        from madsdp_gpu.solver import _MarshalledBatch
+        self.marsh = _MarshalledBatch(list(models))
+        self.stats = (G.Stats * self.marsh.count)()
 
     def __len__(self):
-        return len(self.marsh)
+        return self.marsh.count
 
 
 def solve_many(models, threads: int, seconds: float = 0.0, start: int = 0, count: Optional[int] = None,
@@ -124,9 +123,8 @@ def solve_many(models, threads: int, seconds: float = 0.0, start: int = 0, count
         raise ValueError("range outside the prepared problems")
     for i in range(start, start + n):
         prep.stats[i].status = -2
-    descs = C.cast(C.byref(prep.descs, start * C.sizeof(prep.descs._type_)), C.POINTER(prep.descs._type_))
     stats = C.cast(C.byref(prep.stats, start * C.sizeof(prep.stats._type_)), C.POINTER(prep.stats._type_))
-    lib.msdp_cpu_solve_many(descs, n, threads, seconds, C.byref(_options(lib, options)), stats)
+    lib.msdp_cpu_solve_many(prep.marsh.descs(start), n, threads, seconds, C.byref(_options(lib, options)), stats)
     out = []
     for i in range(start, start + n):
         s = prep.stats[i]
