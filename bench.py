@@ -67,7 +67,7 @@ def _timed_port(prep, start, seconds, cores):
     """Solve the prepared instances from `start` on (cyclically) with the
     compiled CPU restatement on `cores` threads, starting new solves for
     `seconds` and letting the ones in flight finish.  Returns (solves/s,
-    results as (index, status, pobj, iter), next index)."""
+    results as (index, status, pobj, iter, solve ms), next index)."""
     from oracle import cpu_ipm
     n = len(prep)
     nxt, results = start % n, []
@@ -79,7 +79,7 @@ def _timed_port(prep, start, seconds, cores):
         out = cpu_ipm.solve_many(prep, cores, left, start=nxt, count=n - nxt)
         for k, s in enumerate(out):
             if s is not None:
-                results.append((nxt + k, s["status"], s["pobj"], s["iter"]))
+                results.append((nxt + k, s["status"], s["pobj"], s["iter"], s["solve_ns"] / 1e6))
         done = sum(s is not None for s in out)
         nxt = (nxt + done) % n
         if done < len(out):
@@ -95,6 +95,50 @@ def cpu_port_prepare(models):
     prep = cpu_ipm.Prepared(models)
     cpu_ipm.solve_many(prep, 1, 0.0, start=0, count=1)
     return prep
+
+
+def cpu_serve_replay(stream, cores, seconds):
+    """The served stream on the host cores.  Every request is solved by the
+    compiled restatement with all cores busy, in arrival order, new solves
+    starting for `seconds` (the requests solved are a prefix of the
+    stream).  The measured solve times are then scheduled first-in
+    first-out on `cores` workers from the arrival times.  That latency is
+    the one of an ideal CPU server without dispatch overhead (a lower
+    bound); `capacity_solves_per_s` is the solves per second of all cores
+    on this mix."""
+    import heapq
+    import numpy as np
+    from oracle import cpu_ipm
+    prep = cpu_port_prepare([m for _, _, m in stream])
+    t0 = time.perf_counter()
+    res = cpu_ipm.solve_many(prep, cores, seconds)
+    wall = time.perf_counter() - t0
+    k = 0
+    while k < len(res) and res[k] is not None:
+        k += 1
+    free = [0.0] * cores
+    lat, per_kind = [], {}
+    for i in range(k):
+        arrival, kind, _ = stream[i]
+        start = max(arrival, heapq.heappop(free))
+        finish = start + res[i]["solve_ns"] / 1e9
+        heapq.heappush(free, finish)
+        lat.append(finish - arrival)
+        per_kind.setdefault(kind, []).append(finish - arrival)
+    if not k:
+        return {"requests": 0, "of": len(stream), "note": f"no request solved within {seconds:.0f} s"}
+    last = max(free)
+    return {
+        "requests": k, "of": len(stream), "cores": cores,
+        "converged": int(sum(res[i]["status"] == 1 for i in range(k))),
+        "capacity_solves_per_s": k / wall,
+        "solves_per_s": k / max(last - stream[0][0], 1e-9),
+        "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+        "per_kind": {kd: {"count": len(v), "p50_latency_s": float(np.percentile(v, 50)),
+                          "p99_latency_s": float(np.percentile(v, 99))} for kd, v in sorted(per_kind.items())},
+        "method": "compiled C++ restatement solves each request (all cores busy); FIFO schedule of the measured "
+                  "solve times on one worker per core from the arrival times (ideal CPU server, no overhead)",
+    }
 
 
 CPU_PORT = "compiled C++ restatement of the oracle (oracle/cpu_ipm.cpp: FP64, NT+EigenStep+Mehrotra+DenseCholesky, " \
@@ -395,12 +439,14 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     per_step = max(2.0, args.cpu_seconds / max(1, args.steps + args.warmup))
     prep = cpu_port_prepare(models)
-    vals, nxt = [], 0
+    vals, nxt, solve_ms = [], 0, []
     for k in range(args.warmup + args.steps):
-        rate, _, nxt = _timed_port(prep, nxt, per_step, cores)
+        rate, res, nxt = _timed_port(prep, nxt, per_step, cores)
         if k >= args.warmup:
             vals.append(rate)
+            solve_ms += [r[4] for r in res]
     value = statistics.mean(vals)
+    solve_ms.sort()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
@@ -409,7 +455,10 @@ def run_reference(args):
                    "components": "PrimalDual(NT, EigenStep, Mehrotra) + DenseCholesky"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{CPU_PORT} on the workload's instances in order, {per_step:.0f} s per step, "
-                                   f"{cores} threads"},
+                                   f"{cores} threads",
+                         "p50_latency_ms": solve_ms[len(solve_ms) // 2] if solve_ms else None,
+                         "p99_latency_ms": solve_ms[min(len(solve_ms) - 1, int(0.99 * len(solve_ms)))]
+                         if solve_ms else None},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -524,6 +573,8 @@ def run_gpu(args):
                         "mix": "50%% SOS d~U%s, 30%% max-cut n~U%s p=4/n, 20%% dense one block n~U%s m<=min(%d, n(n+1)/2)"
                                % (SERVE_MIX["sos_d"], SERVE_MIX["maxcut_n"], SERVE_MIX["dense_n"], SERVE_MIX["dense_m"]),
                         "latency": "host clock, arrival to result available"})
+        if rank == 0 and world == 1 and not args.no_cpu:
+            serving["cpu_replay"] = cpu_serve_replay(stream, os.cpu_count() or 1, args.cpu_seconds)
 
     if rank != 0:
         return
@@ -546,8 +597,12 @@ def run_gpu(args):
         cpu_block = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": "port",
                      "sample": f"{CPU_PORT}: {cpu['count']} solves of the {args.instances} instances in order "
                                f"(from the first, cyclically), {args.cpu_seconds:.0f} s, {cpu['cores']} threads"}
+        cpu_ms = np.array([r[4] for r in cpu["results"]])
+        if cpu_ms.size:
+            cpu_block["p50_latency_ms"] = float(np.percentile(cpu_ms, 50))
+            cpu_block["p99_latency_ms"] = float(np.percentile(cpu_ms, 99))
         errs = []
-        for i, status, pobj, it in cpu["results"]:
+        for i, status, pobj, it, _ in cpu["results"]:
             s = stm[i]
             errs.append(abs(pobj - s["pobj"]) / max(1.0, abs(s["pobj"]) + abs(s["dobj"])))
         oracle_err = max(errs) if errs else None

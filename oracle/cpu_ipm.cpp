@@ -445,9 +445,37 @@ struct Solver {
 
   // H_jk = sum_i <A_ij, W_i A_ik W_i> + C_lin diag(x/z) C_lin' (lower),
   // then the regularization retry loop (src/solver.jl:299-314)
+  // Per constraint k: T = W A_k W (A_k W by rows, then one product), and
+  // H_jk = A_j(T) for j >= k; cost m (2 n^3 + nnz) + n nnz.
+  void schur_by_columns(const Block& k, Mat& H0) const {
+    const int n = k.n;
+    Mat AW(n), T;
+    for (int c = 0; c < m; ++c) {
+      if (k.cptr[c] == k.cptr[c + 1]) continue;
+      std::fill(AW.a.begin(), AW.a.end(), 0.0);
+      for (int64_t f = k.cptr[c]; f < k.cptr[c + 1]; ++f) {  // row r_f of A_k W += v_f W(c_f, :)
+        const int r = k.row[f], cf = k.col[f];
+        const double v = k.val[f];
+        for (int q = 0; q < n; ++q) AW(r, q) += v * k.W(cf, q);
+      }
+      gemm(k.W, false, AW, false, T);
+      for (int j = c; j < m; ++j) {
+        double s = 0.0;
+        for (int64_t e = k.cptr[j]; e < k.cptr[j + 1]; ++e) s += k.val[e] * T(k.row[e], k.col[e]);
+        H0(j, c) += s;
+      }
+    }
+  }
+
   bool factorize_schur() {
     Mat H0(m);
     for (const auto& k : B) {
+      // the cheaper of the two summation orders of the same sum
+      const double nnz = (double)k.val.size();
+      if (nnz * nnz > 2.0 * (double)m * (2.0 * k.n * (double)k.n * k.n + nnz)) {
+        schur_by_columns(k, H0);
+        continue;
+      }
       for (int j = 0; j < m; ++j)
         for (int c = 0; c <= j; ++c) {
           double s = 0.0;

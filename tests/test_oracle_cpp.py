@@ -57,7 +57,13 @@ def test_maxcut(n, p):
 
 
 def test_dense_mixed_cones():
+    # dense constraints: the per-constraint summation order of the assembly
     agree(g.dense_random([8, 5, 3], 4, 25, seed=3))
+
+
+def test_dense_one_block_served_mix_shape():
+    from madsdp_gpu.serving import _dense_request
+    agree(_dense_request(np.random.default_rng(7), 16, 16, 60, 11))
 
 
 def test_max_iter_status():
