@@ -97,6 +97,19 @@ def cpu_port_prepare(models):
     return prep
 
 
+def fifo_latencies(arrivals, service, workers):
+    """Latency (finish - arrival) of each request served first-in first-out
+    by `workers` identical workers; arrivals in nondecreasing order."""
+    import heapq
+    free = [0.0] * workers
+    out = []
+    for a, t in zip(arrivals, service):
+        start = max(a, heapq.heappop(free))
+        heapq.heappush(free, start + t)
+        out.append(start + t - a)
+    return out
+
+
 def cpu_serve_replay(stream, cores, seconds):
     """The served stream on the host cores.  Every request is solved by the
     compiled restatement with all cores busy, in arrival order, new solves
@@ -106,7 +119,6 @@ def cpu_serve_replay(stream, cores, seconds):
     the one of an ideal CPU server without dispatch overhead (a lower
     bound); `capacity_solves_per_s` is the solves per second of all cores
     on this mix."""
-    import heapq
     import numpy as np
     from oracle import cpu_ipm
     prep = cpu_port_prepare([m for _, _, m in stream])
@@ -116,18 +128,13 @@ def cpu_serve_replay(stream, cores, seconds):
     k = 0
     while k < len(res) and res[k] is not None:
         k += 1
-    free = [0.0] * cores
-    lat, per_kind = [], {}
-    for i in range(k):
-        arrival, kind, _ = stream[i]
-        start = max(arrival, heapq.heappop(free))
-        finish = start + res[i]["solve_ns"] / 1e9
-        heapq.heappush(free, finish)
-        lat.append(finish - arrival)
-        per_kind.setdefault(kind, []).append(finish - arrival)
     if not k:
         return {"requests": 0, "of": len(stream), "note": f"no request solved within {seconds:.0f} s"}
-    last = max(free)
+    lat = fifo_latencies([a for a, _, _ in stream[:k]], [r["solve_ns"] / 1e9 for r in res[:k]], cores)
+    per_kind = {}
+    for (arrival, kind, _), t in zip(stream[:k], lat):
+        per_kind.setdefault(kind, []).append(t)
+    last = max(a + t for (a, _, _), t in zip(stream[:k], lat))
     return {
         "requests": k, "of": len(stream), "cores": cores,
         "converged": int(sum(res[i]["status"] == 1 for i in range(k))),

@@ -37,3 +37,25 @@ def test_reference_arm_single_instance():
     d = run_bench("--workload", "maxcut_n100", "--cpu-seconds", "3")
     check_common(d)
     assert d["value"] > 0 and d["config"]["workload"] == "maxcut_n100"
+
+
+def test_fifo_latencies():
+    sys.path.insert(0, ROOT)
+    import bench
+    # two workers, three simultaneous requests: the third waits for the first
+    assert bench.fifo_latencies([0.0, 0.0, 0.0], [1.0, 2.0, 1.0], 2) == [1.0, 2.0, 2.0]
+    # idle workers: latency = service time
+    assert bench.fifo_latencies([0.0, 5.0, 10.0], [1.0, 1.0, 1.0], 1) == [1.0, 1.0, 1.0]
+    # one worker, a backlog
+    assert bench.fifo_latencies([0.0, 0.5, 1.0], [1.0, 1.0, 1.0], 1) == [1.0, 1.5, 2.0]
+
+
+def test_cpu_serve_replay_small_stream():
+    sys.path.insert(0, ROOT)
+    import bench
+    from madsdp_gpu.serving import poisson_stream
+    stream = poisson_stream(20.0, 1.0, seed=3, sos_d=(5, 12), maxcut_n=(10, 20), dense_n=(6, 10), dense_m=20)
+    r = bench.cpu_serve_replay(stream, 2, 30.0)
+    assert r["requests"] == r["of"] == len(stream) and r["converged"] == r["requests"]
+    assert 0 < r["p50_latency_s"] <= r["p99_latency_s"]
+    assert sum(v["count"] for v in r["per_kind"].values()) == r["requests"]
