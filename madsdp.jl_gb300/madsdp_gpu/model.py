@@ -16,11 +16,11 @@ Storage chosen for the device path:
 * ``C[i]``: dense ``n_i x n_i`` float64 (symmetric).
 * ``A[i]``: the constraint matrices of block ``i`` as a coordinate list
   of *full* symmetric entries (both triangles), sorted by constraint and
-  then by column-major position: arrays ``con, row, col, val``.  A
-  one-hot constraint ``e_k e_k'`` is one entry, a Hankel 0/1 constraint
-  ``sum_{a+b=k} E_ab`` is up to ``n`` entries, a dense constraint is
-  ``n^2`` entries.
-* ``b`` (m), ``d_lin`` (ns), ``C_lin`` (m x ns) dense float64.
+  then by column-major position: arrays ``con, row, col`` (int32) and
+  ``val``.  A one-hot constraint ``e_k e_k'`` is one entry, a Hankel 0/1
+  constraint ``sum_{a+b=k} E_ab`` is up to ``n`` entries, a dense
+  constraint is ``n^2`` entries.
+* ``b`` (m), ``d_lin`` (ns), ``C_lin`` (m x ns, column-major) dense float64.
 """
 
 from __future__ import annotations
@@ -49,10 +49,12 @@ class BlockConstraints:
         order = np.lexsort((row, col, con))
         self.n = int(n)
         self.m = int(m)
-        self.con = con[order]
-        self.row = row[order]
-        self.col = col[order]
-        self.val = val[order]
+        # int32 indices and contiguous values: the layout the C ABI reads,
+        # so that a batch passes these arrays to it without copies
+        self.con = con[order].astype(np.int32)
+        self.row = row[order].astype(np.int32)
+        self.col = col[order].astype(np.int32)
+        self.val = np.ascontiguousarray(val[order])
         # constraint pointer (CSR over constraints)
         self.ptr = np.zeros(m + 1, dtype=np.int64)
         np.add.at(self.ptr, self.con + 1, 1)
@@ -110,7 +112,8 @@ class Model:
         self.ns = int(self.d_lin.size)
         if C_lin is None:
             C_lin = np.zeros((self.m, self.ns))
-        self.C_lin = np.ascontiguousarray(np.asarray(C_lin, dtype=np.float64).reshape(self.m, self.ns))
+        # column-major, the layout of the C ABI
+        self.C_lin = np.asfortranarray(np.asarray(C_lin, dtype=np.float64).reshape(self.m, self.ns))
         if len(A) != len(self.C):
             raise ValueError("one constraint list per PSD block is required")
         blocks = []

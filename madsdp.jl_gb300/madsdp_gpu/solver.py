@@ -170,15 +170,6 @@ class _Marshalled:
         self.desc = d
 
 
-def _cat(parts, dtype) -> np.ndarray:
-    """One contiguous array of `dtype` (at least one element, so that its
-    address is valid) from the flattened parts, converted in the copy."""
-    if not parts:
-        return np.zeros(1, dtype=dtype)
-    out = np.concatenate([np.asarray(a).reshape(-1) for a in parts], dtype=dtype, casting="unsafe")
-    return out if out.size else np.zeros(1, dtype=dtype)
-
-
 def _offsets(sizes: np.ndarray) -> np.ndarray:
     """Exclusive prefix sum, as uint64 element offsets."""
     off = np.zeros(sizes.size, dtype=np.uint64)
@@ -195,57 +186,64 @@ def _desc_dtype() -> np.dtype:
                      "itemsize": C.sizeof(_lib.ProblemDesc)})
 
 
+def _addr(a: np.ndarray) -> int:
+    return a.__array_interface__["data"][0]
+
+
 class _MarshalledBatch:
-    """Many problems packed into a few contiguous arrays, with the table of
-    msdp_problem_desc built as one numpy structured array (each pointer is
-    the base of a packed array plus the problem's or block's offset).  It
-    holds every buffer the descriptors point to while the C call runs."""
+    """The table of msdp_problem_desc of many problems, built as one numpy
+    structured array whose pointers are the addresses of the models' own
+    arrays (a Model stores them in the layout of the C ABI: int32 indices,
+    contiguous float64 values, column-major C_lin), so nothing is copied.
+    An array in another layout is converted and the copy kept here.  C is
+    passed as stored: a C-ordered buffer read column-major is C', and
+    <C, X> for symmetric X and sym(C - A*(y)) are the same for C and C'.
+    Holds every buffer the descriptors point to while the C call runs."""
 
     def __init__(self, models: Sequence[Model]):
         n = len(models)
+        self._keep = []
+
+        def as_is(a, dtype, fortran=False):
+            ok = a.dtype == dtype and (a.flags.f_contiguous if fortran else a.flags.c_contiguous)
+            if not ok:
+                a = np.asfortranarray(a, dtype=dtype) if fortran else np.ascontiguousarray(a, dtype=dtype)
+                self._keep.append(a)
+            return _addr(a)
+
+        def dense(c):
+            if c.dtype == np.float64 and (c.flags.c_contiguous or c.flags.f_contiguous):
+                return _addr(c)
+            return as_is(c, np.float64, fortran=True)
+
         nb = np.fromiter((mm.nblocks for mm in models), dtype=np.int64, count=n)
         ms = np.fromiter((mm.m for mm in models), dtype=np.int64, count=n)
         ns = np.fromiter((mm.ns for mm in models), dtype=np.int64, count=n)
         blocks = [A for mm in models for A in mm.A]
-        self.sides = _cat([np.asarray(mm.sides, dtype=np.int64) for mm in models], np.int32)
-        self.nnz = np.fromiter((A.val.size for A in blocks), dtype=np.int64, count=len(blocks))
-        self.C = _cat([np.asarray(c, dtype=np.float64).ravel(order="F") for mm in models for c in mm.C], np.float64)
-        self.con = _cat([A.con for A in blocks], np.int32)
-        self.row = _cat([A.row for A in blocks], np.int32)
-        self.col = _cat([A.col for A in blocks], np.int32)
-        self.val = _cat([A.val for A in blocks], np.float64)
-        self.b = _cat([mm.b for mm in models], np.float64)
-        self.d = _cat([mm.d_lin for mm in models], np.float64)
-        self.Cl = _cat([np.asarray(mm.C_lin, dtype=np.float64).ravel(order="F") for mm in models], np.float64)
-        if self.nnz.size == 0:
-            self.nnz = np.zeros(1, dtype=np.int64)
-
-        def base(a):
-            return np.uint64(a.ctypes.data)
-
-        sides64 = np.asarray(self.sides[:len(blocks)], dtype=np.int64)
-        coff = _offsets(sides64 * sides64)
-        eoff = _offsets(self.nnz[:len(blocks)])
-        nblk = max(len(blocks), 1)
-        self.Cp = np.zeros(nblk, dtype=np.uint64)
-        self.conp, self.rowp, self.colp, self.valp = (np.zeros(nblk, dtype=np.uint64) for _ in range(4))
-        if blocks:
-            self.Cp[:] = base(self.C) + np.uint64(8) * coff
-            self.conp[:] = base(self.con) + np.uint64(4) * eoff
-            self.rowp[:] = base(self.row) + np.uint64(4) * eoff
-            self.colp[:] = base(self.col) + np.uint64(4) * eoff
-            self.valp[:] = base(self.val) + np.uint64(8) * eoff
+        nblk = len(blocks)
+        self.sides = np.zeros(max(nblk, 1), dtype=np.int32)
+        self.nnz = np.zeros(max(nblk, 1), dtype=np.int64)
+        self.Cp, self.conp, self.rowp, self.colp, self.valp = (np.zeros(max(nblk, 1), dtype=np.uint64)
+                                                                for _ in range(5))
+        if nblk:
+            self.sides[:] = [s for mm in models for s in mm.sides]
+            self.nnz[:] = [A.val.size for A in blocks]
+            self.Cp[:] = [dense(c) for mm in models for c in mm.C]
+            self.conp[:] = [as_is(A.con, np.int32) for A in blocks]
+            self.rowp[:] = [as_is(A.row, np.int32) for A in blocks]
+            self.colp[:] = [as_is(A.col, np.int32) for A in blocks]
+            self.valp[:] = [as_is(A.val, np.float64) for A in blocks]
         boff = _offsets(nb)
         d = np.zeros(n, dtype=_desc_dtype())
         d["nblocks"], d["m"], d["ns"] = nb, ms, ns
-        d["sides"] = base(self.sides) + np.uint64(4) * boff
-        d["A_nnz"] = base(self.nnz) + np.uint64(8) * boff
+        d["sides"] = np.uint64(_addr(self.sides)) + np.uint64(4) * boff
+        d["A_nnz"] = np.uint64(_addr(self.nnz)) + np.uint64(8) * boff
         for field, arr in (("C", self.Cp), ("A_con", self.conp), ("A_row", self.rowp), ("A_col", self.colp),
                            ("A_val", self.valp)):
-            d[field] = base(arr) + np.uint64(8) * boff
-        d["b"] = base(self.b) + np.uint64(8) * _offsets(ms)
-        d["d_lin"] = base(self.d) + np.uint64(8) * _offsets(ns)
-        d["C_lin"] = base(self.Cl) + np.uint64(8) * _offsets(ms * ns)
+            d[field] = np.uint64(_addr(arr)) + np.uint64(8) * boff
+        d["b"] = [as_is(mm.b, np.float64) for mm in models]
+        d["d_lin"] = [as_is(mm.d_lin, np.float64) for mm in models]
+        d["C_lin"] = [as_is(mm.C_lin, np.float64, fortran=True) for mm in models]
         self.table = d
         self.count = n
 

@@ -173,9 +173,9 @@ class _BlockOp:
     def __init__(self, blk):
         n, m = blk.n, blk.m
         self.n, self.m = n, m
-        self.con = np.asarray(blk.con)
-        self.row = np.asarray(blk.row)
-        self.col = np.asarray(blk.col)
+        self.con = np.asarray(blk.con, dtype=np.int64)
+        self.row = np.asarray(blk.row, dtype=np.int64)
+        self.col = np.asarray(blk.col, dtype=np.int64)
         self.val = np.asarray(blk.val)
         self.nnz = self.val.size
         self.sp = sp.csr_matrix((self.val, (self.con, self.row * n + self.col)), shape=(m, n * n))

@@ -57,6 +57,26 @@ def test_packed_table_equals_per_problem_descriptors():
         same(read_desc(packed.descs(k)[0]), read_desc(single.desc))
 
 
+def test_no_copies_of_model_arrays():
+    models = mixed_models()
+    packed = _MarshalledBatch(models)
+    assert packed._keep == []
+    d = packed.descs(0)[0]
+    A = models[0].A[0]
+    assert C.addressof(d.A_con[0].contents) == A.con.ctypes.data
+    assert C.addressof(d.A_val[0].contents) == A.val.ctypes.data
+
+
+def test_other_layouts_are_converted():
+    m = g.dense_random([5, 3], 3, 6, seed=1)
+    m.C_lin = np.ascontiguousarray(m.C_lin)  # row-major: converted
+    m.A[1].con = m.A[1].con.astype(np.int64)  # wider indices: converted
+    ref = _Marshalled(m)
+    packed = _MarshalledBatch([m])
+    assert len(packed._keep) == 2
+    same(read_desc(packed.descs(0)[0]), read_desc(ref.desc))
+
+
 def test_descs_range_checked():
     packed = _MarshalledBatch(mixed_models()[:2])
     with pytest.raises(IndexError):
