@@ -20,6 +20,7 @@
 
 #include "../../include/madsdp_gpu.h"
 #include "launch.h"
+#include "stage.h"
 
 struct msdp_context;  // defined in capi.cu; a server runs on its own streams
 
@@ -52,20 +53,17 @@ struct Staged {
 // Layout and host image of one problem (same device format as
 // msdp_batch_create: sorted coordinate lists, position lists, Hankel flag,
 // data norms).
-int stage_problem(const msdp_problem_desc& d, const Params& prm, bool mixed, Staged& st) {
+int stage_request(const msdp_problem_desc& d, const Params& prm, bool mixed, Staged& st) {
   if (d.nblocks < 0 || d.m < 0 || d.ns < 0 || (d.nblocks == 0 && d.ns == 0)) return MSDP_ERR_INVALID_ARGUMENT;
   if (d.nblocks > kMaxBlocks) return MSDP_ERR_TOO_LARGE;
   const int nb = d.nblocks;
   const int64_t m = d.m, ns = d.ns;
   st.nblocks = nb; st.m = d.m; st.ns = d.ns;
   st.sides.assign(d.sides, d.sides + nb);
-  int64_t nnz_total = 0, ptr_total = 0, dd_len = m + ns + m * ns + 3;
+  int64_t nnz_total = 0;
   for (int i = 0; i < nb; ++i) {
-    const int64_t n = d.sides[i];
-    if (n <= 0 || d.A_nnz[i] < 0) return MSDP_ERR_INVALID_ARGUMENT;
+    if (d.sides[i] <= 0 || d.A_nnz[i] < 0) return MSDP_ERR_INVALID_ARGUMENT;
     nnz_total += d.A_nnz[i];
-    ptr_total += m + 1 + n * n + 1;
-    dd_len += n * n;
   }
   // element offsets inside the typed sections
   ProbDesc& pd = st.pd;
@@ -108,69 +106,12 @@ int stage_problem(const msdp_problem_desc& d, const Params& prm, bool mixed, Sta
   st.nnz = nnz_total;
   st.erow.assign(nnz_total, 0); st.ecol.assign(nnz_total, 0); st.pcon.assign(nnz_total, 0);
   st.eval.assign(nnz_total, 0.0); st.pval.assign(nnz_total, 0.0);
-  double* hdd = (double*)(st.image.data() + st.o_dd);
-  int32_t* herow = st.erow.data();
-  int32_t* hecol = st.ecol.data();
-  int32_t* hpcon = st.pcon.data();
-  double* heval = st.eval.data();
-  double* hpval = st.pval.data();
-  int64_t* hptr = (int64_t*)(st.image.data() + st.o_ptr);
-  double bn = 0.0, dn = 0.0, cmax = 0.0;
-  for (int64_t j = 0; j < m; ++j) { hdd[j] = d.b[j]; bn = std::max(bn, std::fabs(d.b[j])); }
-  for (int64_t k = 0; k < ns; ++k) { hdd[m + k] = d.d_lin[k]; dn = std::max(dn, std::fabs(d.d_lin[k])); }
-  for (int64_t k = 0; k < m * ns; ++k) hdd[m + ns + k] = d.C_lin[k];
-  for (int i = 0; i < nb; ++i) {
-    BlockDesc& bd = st.bd[i];
-    const int64_t n = bd.n, nn = n * n, nnz = bd.nnz;
-    double cn = 0.0;
-    for (int64_t k = 0; k < nn; ++k) { hdd[bd.cdat + k] = d.C[i][k]; cn = std::max(cn, std::fabs(d.C[i][k])); }
-    bd.cnorm = cn;
-    cmax = std::max(cmax, cn);
-    const int32_t *con = d.A_con[i], *row = d.A_row[i], *col = d.A_col[i];
-    const double* val = d.A_val[i];
-    for (int64_t e = 0; e < nnz; ++e)
-      if (con[e] < 0 || con[e] >= m || row[e] < 0 || row[e] >= n || col[e] < 0 || col[e] >= n)
-        return MSDP_ERR_INVALID_ARGUMENT;
-    std::vector<int64_t> idx(nnz);
-    std::iota(idx.begin(), idx.end(), 0);
-    std::sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) {
-      if (con[a] != con[b]) return con[a] < con[b];
-      if (col[a] != col[b]) return col[a] < col[b];
-      return row[a] < row[b];
-    });
-    int64_t* cptr = hptr + bd.conptr;
-    for (int64_t e = 0; e < nnz; ++e) {
-      const int64_t s = idx[e];
-      herow[bd.ent + e] = row[s]; hecol[bd.ent + e] = col[s]; heval[bd.ent + e] = val[s];
-      cptr[con[s] + 1] += 1;
-    }
-    for (int64_t j = 0; j < m; ++j) cptr[j + 1] += cptr[j];
-    bool hankel = (m == 2 * n - 1) && nnz == n * n;
-    for (int64_t j = 0; hankel && j < m; ++j) {
-      const int64_t lo = std::max<int64_t>(0, j - n + 1), hi = std::min<int64_t>(j, n - 1);
-      if (cptr[j + 1] - cptr[j] != hi - lo + 1) { hankel = false; break; }
-      int64_t prev = -1;
-      for (int64_t q = cptr[j]; q < cptr[j + 1]; ++q) {
-        const int64_t e = bd.ent + q;
-        if (herow[e] + hecol[e] != j || heval[e] != 1.0 || hecol[e] <= prev) { hankel = false; break; }
-        prev = hecol[e];
-      }
-    }
-    bd.structure = choose_structure(hankel, n, m, nnz);
-    int64_t* pptr = hptr + bd.posptr;
-    for (int64_t e = 0; e < nnz; ++e) pptr[row[e] + (int64_t)col[e] * n + 1] += 1;
-    for (int64_t k = 0; k < nn; ++k) pptr[k + 1] += pptr[k];
-    std::vector<int64_t> fill(pptr, pptr + nn);
-    for (int64_t e = 0; e < nnz; ++e) {
-      const int64_t s = idx[e];
-      const int64_t q = fill[row[s] + (int64_t)col[s] * n]++;
-      hpcon[bd.ent + q] = con[s]; hpval[bd.ent + q] = val[s];
-    }
-  }
-  hdd[m + ns + m * ns + 0] = bn;
-  hdd[m + ns + m * ns + 1] = dn;
-  hdd[m + ns + m * ns + 2] = cmax;
-  (void)dd_len;
+  // the problem's data range is the whole dd section, its entries and
+  // pointers the whole lists (stage.h)
+  const StageBuffers sb{(double*)(st.image.data() + st.o_dd), dd, st.erow.data(), st.ecol.data(), st.eval.data(),
+                        st.pcon.data(), st.pval.data(), (int64_t*)(st.image.data() + st.o_ptr)};
+  std::vector<int64_t> idx, fill;
+  if (!::stage_problem(d, pd, st.bd, dd, sb, idx, fill)) return MSDP_ERR_INVALID_ARGUMENT;
   return MSDP_OK;
 }
 
@@ -557,7 +498,7 @@ int msdp_server_destroy(msdp_server* s) {
 int msdp_server_submit(msdp_server* s, const msdp_problem_desc* prob, int64_t* request_id) {
   if (!s || !prob || !request_id) return MSDP_ERR_INVALID_ARGUMENT;
   auto r = std::make_unique<Request>();
-  const int rc = stage_problem(*prob, s->prm, s->mixed, r->st);
+  const int rc = stage_request(*prob, s->prm, s->mixed, r->st);
   if (rc) return rc;
   if (r->st.total_bytes > s->arena_bytes || r->st.nnz > s->entry_capacity) return MSDP_ERR_TOO_LARGE;
   r->id = s->next_id++;
