@@ -79,6 +79,8 @@ def _timed_port(prep, start, seconds, cores):
         out = cpu_ipm.solve_many(prep, cores, left, start=nxt, count=n - nxt)
         for k, s in enumerate(out):
             if s is not None:
+                if s["status"] < 0:
+                    raise RuntimeError(f"the CPU restatement rejected instance {nxt + k}")
                 results.append((nxt + k, s["status"], s["pobj"], s["iter"], s["solve_ns"] / 1e6))
         done = sum(s is not None for s in out)
         nxt = (nxt + done) % n
@@ -146,6 +148,42 @@ def cpu_serve_replay(stream, cores, seconds):
         "method": "compiled C++ restatement solves each request (all cores busy); FIFO schedule of the measured "
                   "solve times on one worker per core from the arrival times (ideal CPU server, no overhead)",
     }
+
+
+def cpu_batch_sample(args):
+    """The batched workload on the host cores: all cores for `cpu_seconds`
+    over the instances in order, then one thread for a quarter of that on
+    the instances after them."""
+    cores = os.cpu_count() or 1
+    prep = cpu_port_prepare(workload(args.instances, args.seed)[0])
+    v, res, nxt = _timed_port(prep, 0, args.cpu_seconds, cores)
+    v1, res1, _ = _timed_port(prep, nxt, max(2.0, args.cpu_seconds / 4), 1)
+    return {"value": v, "results": res, "count": len(res), "cores": cores, "one_thread": v1,
+            "one_thread_count": len(res1)}
+
+
+def cpu_batch_block(cpu, args, gpu_stats):
+    """(cpu_baseline object of the line, largest relative objective
+    difference between the GPU stats and the CPU solves of the same
+    instances); (None, None) without a CPU sample."""
+    import numpy as np
+    if cpu is None:
+        return None, None
+    block = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": "port",
+             "sample": f"{CPU_PORT}: {cpu['count']} solves of the {args.instances} instances in order "
+                       f"(from the first, cyclically), {args.cpu_seconds:.0f} s, {cpu['cores']} threads",
+             "one_thread_solves_per_s": cpu["one_thread"],
+             "one_thread_sample": f"the next {cpu['one_thread_count']} instances on one thread, "
+                                  f"{max(2.0, args.cpu_seconds / 4):.0f} s"}
+    cpu_ms = np.array([r[4] for r in cpu["results"]])
+    if cpu_ms.size:
+        block["p50_latency_ms"] = float(np.percentile(cpu_ms, 50))
+        block["p99_latency_ms"] = float(np.percentile(cpu_ms, 99))
+    errs = []
+    for i, status, pobj, it, _ in cpu["results"]:
+        s = gpu_stats[i]
+        errs.append(abs(pobj - s["pobj"]) / max(1.0, abs(s["pobj"]) + abs(s["dobj"])))
+    return block, (max(errs) if errs else None)
 
 
 CPU_PORT = "compiled C++ restatement of the oracle (oracle/cpu_ipm.cpp: FP64, NT+EigenStep+Mehrotra+DenseCholesky, " \
@@ -480,11 +518,7 @@ def run_gpu(args):
     # CPU baseline first, on the host cores before any CUDA work
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cores = os.cpu_count() or 1
-        prep = cpu_port_prepare(workload(args.instances, args.seed)[0])
-        v, res, _ = _timed_port(prep, 0, args.cpu_seconds, cores)
-        cpu = {"value": v, "results": res, "count": len(res), "cores": cores}
-        del prep
+        cpu = cpu_batch_sample(args)
 
     import torch
     import torch.distributed as dist
@@ -598,21 +632,7 @@ def run_gpu(args):
     hbm, bf16, peak_kind = measured_peaks()
     achieved = flops / kern_s / 1e12
     traffic = profiled_traffic()
-    cpu_block = None
-    oracle_err = None
-    if cpu is not None:
-        cpu_block = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": "port",
-                     "sample": f"{CPU_PORT}: {cpu['count']} solves of the {args.instances} instances in order "
-                               f"(from the first, cyclically), {args.cpu_seconds:.0f} s, {cpu['cores']} threads"}
-        cpu_ms = np.array([r[4] for r in cpu["results"]])
-        if cpu_ms.size:
-            cpu_block["p50_latency_ms"] = float(np.percentile(cpu_ms, 50))
-            cpu_block["p99_latency_ms"] = float(np.percentile(cpu_ms, 99))
-        errs = []
-        for i, status, pobj, it, _ in cpu["results"]:
-            s = stm[i]
-            errs.append(abs(pobj - s["pobj"]) / max(1.0, abs(s["pobj"]) + abs(s["dobj"])))
-        oracle_err = max(errs) if errs else None
+    cpu_block, oracle_err = cpu_batch_block(cpu, args, stm)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,

@@ -203,6 +203,8 @@ class _MarshalledBatch:
     def __init__(self, models: Sequence[Model]):
         n = len(models)
         self._keep = []
+        # the descriptors point into these models' arrays: keep them alive
+        self.models = list(models)
 
         def as_is(a, dtype, fortran=False):
             ok = a.dtype == dtype and (a.flags.f_contiguous if fortran else a.flags.c_contiguous)

@@ -59,3 +59,22 @@ def test_cpu_serve_replay_small_stream():
     assert r["requests"] == r["of"] == len(stream) and r["converged"] == r["requests"]
     assert 0 < r["p50_latency_s"] <= r["p99_latency_s"]
     assert sum(v["count"] for v in r["per_kind"].values()) == r["requests"]
+
+
+def test_cpu_batch_baseline_block():
+    """The GPU line's CPU leg, with the CPU solves standing in for the GPU
+    stats: the block carries the contract's keys and a zero difference."""
+    sys.path.insert(0, ROOT)
+    import argparse
+
+    import bench
+    from oracle import cpu_ipm
+    args = argparse.Namespace(instances=24, seed=4, cpu_seconds=3.0)
+    cpu = bench.cpu_batch_sample(args)
+    models = bench.workload(args.instances, args.seed)[0]
+    stats = cpu_ipm.solve_many(models, threads=2)
+    block, err = bench.cpu_batch_block(cpu, args, stats)
+    assert block["kind"] == "port" and block["value"] > 0 and block["one_thread_solves_per_s"] > 0
+    assert 0 < block["p50_latency_ms"] <= block["p99_latency_ms"]
+    assert err == 0.0
+    assert bench.cpu_batch_block(None, args, stats) == (None, None)

@@ -81,3 +81,14 @@ def test_descs_range_checked():
     packed = _MarshalledBatch(mixed_models()[:2])
     with pytest.raises(IndexError):
         packed.descs(3)
+
+
+def test_table_keeps_the_models_alive():
+    import gc
+    packed = _MarshalledBatch([g.sos_hankel(6, seed=9), build("mixed_lp")])
+    gc.collect()
+    for _ in range(50):  # churn the allocator
+        np.ones(1000)
+    d = read_desc(packed.descs(0)[0])
+    ref = g.sos_hankel(6, seed=9)
+    assert np.array_equal(d["blocks"][0]["con"], ref.A[0].con) and np.array_equal(d["b"], ref.b)
