@@ -275,6 +275,39 @@ def cpu_instance_sample(spec, seed, seconds):
     return (statistics.mean(iters) if iters else None), len(iters), init
 
 
+# instances whose solve the compiled restatement (own dense kernels, no
+# BLAS) finishes in about a second: timed with it, larger ones with the
+# NumPy oracle on all BLAS threads
+PORT_MAX_FLOPS_PER_SOLVE = 5e9
+
+
+def port_fits(model) -> bool:
+    return 20 * instance_flops_per_iteration(model) <= PORT_MAX_FLOPS_PER_SOLVE
+
+
+def cpu_port_instance(model, seconds):
+    """Full solves of one instance by the compiled restatement on one
+    thread, repeated for about `seconds` (at least one); returns (solves/s,
+    solves, iterations of a solve)."""
+    from oracle import cpu_ipm
+    cpu_ipm.build()
+    cpu_ipm.solve(model)  # load, untimed
+    done, t0 = 0, time.perf_counter()
+    while True:
+        st = cpu_ipm.solve(model)
+        if st["status"] < 0:
+            raise RuntimeError("the CPU restatement rejected the instance")
+        done += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    return done / (time.perf_counter() - t0), done, st["iter"]
+
+
+def port_block(v, done, iters):
+    return {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{CPU_PORT}: {done} full solves of the same instance on one thread ({iters} iterations)"}
+
+
 def run_instance_reference(args):
     """The oracle on the same large instance, all BLAS threads: a bounded
     number of iterations, solve time = init + mean iteration x iterations to
@@ -283,13 +316,20 @@ def run_instance_reference(args):
     if int(os.environ.get("RANK", "0")) != 0:
         return
     spec = INSTANCE_WORKLOADS[args.workload]
-    per_it, nit, init = cpu_instance_sample(spec, args.seed, args.cpu_seconds)
-    iters = {"maxcut_n100": 11, "maxcut_n2000": 16, "dense_mixed_cones": 18}[args.workload]
     cores = os.cpu_count() or 1
     line = {"impl": "reference", "metric": METRIC, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": args.workload, **{k: v for k, v in spec.items() if k != "kind"},
                                             "seed": args.seed}}
+    model = instance_model(spec, args.seed)
+    if port_fits(model):
+        v, done, it = cpu_port_instance(model, args.cpu_seconds)
+        line.update(value=v, cpu_baseline=port_block(v, done, it))
+        line["e2e"] = {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+        print(json.dumps(line), flush=True)
+        return
+    per_it, nit, init = cpu_instance_sample(spec, args.seed, args.cpu_seconds)
+    iters = {"maxcut_n100": 11, "maxcut_n2000": 16, "dense_mixed_cones": 18}[args.workload]
     if per_it is None:
         line.update(value=None, cpu_baseline={"value": None, "unit": UNIT, "cores": cores, "kind": "port",
                                               "sample": f"no oracle iteration finished within {args.cpu_seconds:.0f} s"})
@@ -306,9 +346,14 @@ def run_instance(args):
     """One large problem per step on the whole GPU (msdp_solver)."""
     import numpy as np
     spec = INSTANCE_WORKLOADS[args.workload]
-    cpu = None
+    cpu = port = None
     if not args.no_cpu:
-        cpu = cpu_instance_sample(spec, args.seed, args.cpu_seconds)
+        small = instance_model(spec, args.seed)
+        if port_fits(small):
+            port = cpu_port_instance(small, args.cpu_seconds)
+        else:
+            cpu = cpu_instance_sample(spec, args.seed, args.cpu_seconds)
+        del small
     import torch
     import __graft_entry__
     __graft_entry__.build()
@@ -361,7 +406,7 @@ def run_instance(args):
     t_solve = statistics.mean(ms) / 1000.0
     flops = instance_flops_per_iteration(model) * st["iter"]
     fp64_peak = 1.25e3  # GB300 FP64 nominal, GFLOP/s
-    cpu_block = None
+    cpu_block = port_block(*port) if port is not None else None
     if cpu is not None:
         per_it, nit, init = cpu
         if per_it is not None:
