@@ -1,7 +1,8 @@
-// CPU restatement (C++) of MadSDP's PrimalDual interior-point method with
-// the NT direction, EigenStep, Mehrotra centering, DenseCholesky and the
-// ScaledIdentity start, for timing the CPU baseline of the batched workloads
-// without interpreter overhead.
+// CPU restatement (C++) of MadSDP's PrimalDual interior-point method (NT or
+// HKM direction, EigenStep or CholeskyBacktrack, Mehrotra or AdaptiveMu
+// centering) with DenseCholesky and the ScaledIdentity start, for timing the
+// CPU baseline without interpreter overhead and for checking GPU results at
+// sizes the NumPy restatement is slow on.
 //
 // TEST INFRASTRUCTURE ONLY, like oracle/madsdp_oracle.py, whose algorithm it
 // follows step by step (that module cites the reference file:line of each
@@ -315,7 +316,8 @@ struct Solver {
   double pobj = 0.0, dobj = 0.0, inf_pr = 0.0, inf_du = 0.0, gap = 0.0;
   int iter = 0, status = MSDP_INITIAL;
   msdp_options opt{};
-  double tau = 0.95, sigma_exponent = 3.0;
+  msdp_components comp{};
+  bool nt = true;  // NT or HKM
 
   int nu() const {
     int v = ns;
@@ -407,11 +409,16 @@ struct Solver {
     if (status == MSDP_REGULAR && mu < opt.mu_min) status = MSDP_SEARCH_DIRECTION_BECOMES_TOO_SMALL;
   }
 
-  // NT scaling (src/directions.jl:45-75) and S^-1 (src/primal_dual.jl:29-37)
+  // S^-1 (src/primal_dual.jl:29-37), the NT scaling (src/directions.jl:45-75)
+  // and the Cholesky factor of X that EigenStep uses
   bool prepare() {
     for (auto& k : B) {
       if (!chol_factor(k.S, k.Ls)) return false;
       inverse_from_chol(k.Ls, k.Si);
+      if (!nt) {
+        if (comp.step == MSDP_EIGEN_STEP && !chol_factor(k.X, k.Lx)) return false;
+        continue;
+      }
       if (!chol_factor(k.X, k.Lx)) return false;
       Mat M, N, V;
       gemm(k.Ls, true, k.Lx, false, M);
@@ -445,20 +452,27 @@ struct Solver {
 
   // H_jk = sum_i <A_ij, W_i A_ik W_i> + C_lin diag(x/z) C_lin' (lower),
   // then the regularization retry loop (src/solver.jl:299-314)
-  // Per constraint k: T = W A_k W (A_k W by rows, then one product), and
+  // H_jk = <A_j, L A_k R>: (L, R) = (W, W) for NT, (S^-1, X) for HKM
+  // (src/directions.jl:212,247); both symmetric.
+  const Mat& scale_L(const Block& k) const { return nt ? k.W : k.Si; }
+  const Mat& scale_R(const Block& k) const { return nt ? k.W : k.X; }
+
+  // Per constraint k: T = L A_k R (A_k R by rows, then one product), and
   // H_jk = A_j(T) for j >= k; cost m (2 n^3 + nnz) + n nnz.
   void schur_by_columns(const Block& k, Mat& H0) const {
     const int n = k.n;
-    Mat AW(n), T;
+    const Mat& L = scale_L(k);
+    const Mat& R = scale_R(k);
+    Mat AR(n), T;
     for (int c = 0; c < m; ++c) {
       if (k.cptr[c] == k.cptr[c + 1]) continue;
-      std::fill(AW.a.begin(), AW.a.end(), 0.0);
-      for (int64_t f = k.cptr[c]; f < k.cptr[c + 1]; ++f) {  // row r_f of A_k W += v_f W(c_f, :)
+      std::fill(AR.a.begin(), AR.a.end(), 0.0);
+      for (int64_t f = k.cptr[c]; f < k.cptr[c + 1]; ++f) {  // row r_f of A_k R += v_f R(c_f, :)
         const int r = k.row[f], cf = k.col[f];
         const double v = k.val[f];
-        for (int q = 0; q < n; ++q) AW(r, q) += v * k.W(cf, q);
+        for (int q = 0; q < n; ++q) AR(r, q) += v * R(cf, q);
       }
-      gemm(k.W, false, AW, false, T);
+      gemm(L, false, AR, false, T);
       for (int j = c; j < m; ++j) {
         double s = 0.0;
         for (int64_t e = k.cptr[j]; e < k.cptr[j + 1]; ++e) s += k.val[e] * T(k.row[e], k.col[e]);
@@ -482,9 +496,9 @@ struct Solver {
           for (int64_t e = k.cptr[j]; e < k.cptr[j + 1]; ++e) {
             const int re = k.row[e], ce = k.col[e];
             double t = 0.0;
-            // W is symmetric: W(r_e, r_f) read as W(r_f, r_e), down column r_e
-            const double* wr = &k.W.a[(size_t)re * k.n];
-            const double* wc = &k.W.a[(size_t)ce * k.n];
+            // L(r_e, r_f) R(c_f, c_e), L symmetric: both read down a column
+            const double* wr = &scale_L(k).a[(size_t)re * k.n];
+            const double* wc = &scale_R(k).a[(size_t)ce * k.n];
             for (int64_t f = k.cptr[c]; f < k.cptr[c + 1]; ++f) t += k.val[f] * wr[k.row[f]] * wc[k.col[f]];
             s += k.val[e] * t;
           }
@@ -520,11 +534,11 @@ struct Solver {
     }
   }
 
-  // E(M) = sym(W M W) (src/directions.jl:80-84)
-  static void apply_E(const Block& k, const Mat& M, Mat& out) {
+  // E(M): NT sym(W M W), HKM sym(X M S^-1) (src/directions.jl:80-84,116-120)
+  void apply_E(const Block& k, const Mat& M, Mat& out) const {
     Mat t;
-    gemm(k.W, false, M, false, t);
-    gemm(t, false, k.W, false, out);
+    gemm(nt ? k.W : k.X, false, M, false, t);
+    gemm(t, false, nt ? k.W : k.Si, false, out);
     sym(out);
   }
 
@@ -583,10 +597,19 @@ struct Solver {
     }
   }
 
-  // Mehrotra second-order term, NT (src/step.jl:128-136, src/directions.jl:90-100)
+  // Mehrotra second-order term (src/step.jl:128-136): NT
+  // src/directions.jl:90-100, HKM sym(-(dX dS) S^-1) (:123-127)
   void correction() {
     for (auto& k : B) {
       const int n = k.n;
+      if (!nt) {
+        Mat t;
+        gemm(k.dX, false, k.dS, false, t);
+        gemm(t, false, k.Si, false, k.corr);
+        for (double& v : k.corr.a) v = -v;
+        sym(k.corr);
+        continue;
+      }
       Mat t1, t2, Mm;
       gemm(k.Gi, false, k.dX, false, t1);
       gemm(t1, false, k.dS, false, t2);
@@ -614,7 +637,7 @@ struct Solver {
     Vec w;
     if (!symeig(Zt, w, nullptr)) return 0.0;
     const double lam = w.empty() ? INFINITY : w[0];
-    return lam > -std::sqrt(kEps) ? 1.0 : std::min(1.0, -tau / lam);
+    return lam > -std::sqrt(kEps) ? 1.0 : std::min(1.0, -comp.tau / lam);
   }
 
   static double max_scalar_step(const Vec& v, const Vec& dv) {
@@ -624,7 +647,39 @@ struct Solver {
     return a;
   }
 
+  // LAPACK potrf on the lower triangle of M + a D succeeds (src/blocks.jl:133-137)
+  static bool is_posdef(const Mat& M, double a, const Mat& D) {
+    Mat T(M.n);
+    for (size_t q = 0; q < T.a.size(); ++q) {
+      T.a[q] = M.a[q] + a * D.a[q];
+      if (!std::isfinite(T.a[q])) return false;
+    }
+    return potrf(T);
+  }
+
+  // CholeskyBacktrack (src/step.jl:202-221)
+  double backtrack(bool primal) const {
+    double a = 1.0;
+    for (const auto& k : B) {
+      const Mat& M = primal ? k.X : k.S;
+      const Mat& D = primal ? k.dX : k.dS;
+      while (!is_posdef(M, a, D)) {
+        a *= comp.shrink;
+        if (a < kEps) return 0.0;
+      }
+    }
+    if (a != 1.0) a *= comp.boundary;
+    if (ns) a = std::min(a, comp.boundary * max_scalar_step(primal ? x : z, primal ? dx : dz));
+    return a;
+  }
+
+  // src/step.jl:148-228
   void step_lengths(double& a, double& bt) const {
+    if (comp.step == MSDP_CHOLESKY_BACKTRACK) {
+      a = backtrack(true);
+      bt = backtrack(false);
+      return;
+    }
     a = 1.0;
     bt = 1.0;
     for (const auto& k : B) {
@@ -632,8 +687,8 @@ struct Solver {
       bt = std::min(bt, eigen_step(k.Ls, k.dS));
     }
     if (ns) {
-      a = std::min(a, tau * max_scalar_step(x, dx));
-      bt = std::min(bt, tau * max_scalar_step(z, dz));
+      a = std::min(a, comp.tau * max_scalar_step(x, dx));
+      bt = std::min(bt, comp.tau * max_scalar_step(z, dz));
     }
   }
 
@@ -683,7 +738,7 @@ struct Solver {
     double aa = 0.0, ba = 0.0;
     step_lengths(aa, ba);
     const double mua = affine_complementarity(aa, ba);
-    sigma = std::min(std::max(std::pow(mua / std::max(mu0, kEps), sigma_exponent), 1e-8), 1.0);
+    sigma = std::min(std::max(std::pow(mua / std::max(mu0, kEps), comp.sigma_exponent), 1e-8), 1.0);
     correction();
     solve_directions(sigma * mu0, true);
     double a = 0.0, bt = 0.0;
@@ -691,11 +746,30 @@ struct Solver {
     take_step(a, bt);
   }
 
+  // src/primal_dual.jl:104-121
+  void iterate_adaptive() {
+    if (!prepare() || !factorize_schur()) {
+      status = MSDP_ERROR_IN_STEP_COMPUTATION;
+      return;
+    }
+    solve_directions(mu, false);
+    double a = 0.0, bt = 0.0;
+    step_lengths(a, bt);
+    take_step(a, bt);
+    double m1 = comp.ratio * total_complementarity() / std::max(nu(), 1);
+    if (std::min(a, bt) < 0.5) m1 *= 1.5;
+    if (a + bt > 1.6) m1 *= 0.75;
+    if (a + bt > 1.9) m1 /= 1 + 0.1 * iter;
+    mu = m1;
+  }
+
   // ScaledIdentity start (src/solver.jl:214-233) and solve! (:385-396)
   void solve() {
     double cs = cmax;
     if (ns) cs = std::max(cs, dn);
-    const double beta0 = std::max(10.0, std::sqrt(std::max(bn, 1.0) * std::max(cs, 1.0)) * std::sqrt((double)nu()));
+    const double beta0 = comp.scale > 0.0
+                             ? comp.scale
+                             : std::max(10.0, std::sqrt(std::max(bn, 1.0) * std::max(cs, 1.0)) * std::sqrt((double)nu()));
     for (auto& k : B) {
       k.X = Mat(k.n);
       k.S = Mat(k.n);
@@ -707,10 +781,12 @@ struct Solver {
     iter = 0;
     status = MSDP_REGULAR;
     update_residuals();
-    mu = total_complementarity() / std::max(nu(), 1);
+    mu = total_complementarity() / std::max(nu(), 1);  // src/primal_dual.jl:10-19
+    if (comp.centering == MSDP_ADAPTIVE_MU) mu *= comp.initial_ratio;
     update_termination();
     while (status == MSDP_REGULAR) {
-      iterate_mehrotra();
+      if (comp.centering == MSDP_ADAPTIVE_MU) iterate_adaptive();
+      else iterate_mehrotra();
       if (status != MSDP_REGULAR) break;
       update_termination();
     }
@@ -775,13 +851,45 @@ void msdp_cpu_default_options(msdp_options* o) {
   o->mixed_refine = 2;
 }
 
-// One solve with `opt` (the defaults when null); writes status, iter, the
-// objectives, the three termination measures, mu, sigma, alpha, beta and
-// the wall time of the solve in solve_ns.
-int msdp_cpu_solve(const msdp_problem_desc* d, const msdp_options* opt, msdp_stats* out) {
+// The defaults of src/components.jl (PrimalDual, NT, EigenStep(0.95),
+// Mehrotra(3), ScaledIdentity(), DenseCholesky; CholeskyBacktrack(0.8,
+// 0.95), AdaptiveMu(1/4, 1/2)).
+void msdp_cpu_default_components(msdp_components* c) {
+  std::memset(c, 0, sizeof(*c));
+  c->algorithm = MSDP_PRIMAL_DUAL;
+  c->direction = MSDP_NT;
+  c->step = MSDP_EIGEN_STEP;
+  c->centering = MSDP_MEHROTRA;
+  c->initial_point = MSDP_SCALED_IDENTITY;
+  c->schur = MSDP_DENSE_CHOLESKY;
+  c->precision = MSDP_FP64;
+  c->centering_max_iter = 50;
+  c->tau = 0.95;
+  c->shrink = 0.8;
+  c->boundary = 0.95;
+  c->sigma_exponent = 3.0;
+  c->initial_ratio = 0.25;
+  c->ratio = 0.5;
+  c->scale = 0.0;
+}
+
+// One solve with `comp` and `opt` (the defaults when null); writes status,
+// iter, the objectives, the three termination measures, mu, sigma, alpha,
+// beta and the wall time of the solve in solve_ns.  Components other than
+// PrimalDual with DenseCholesky from ScaledIdentity: MSDP_ERR_UNSUPPORTED.
+int msdp_cpu_solve(const msdp_problem_desc* d, const msdp_components* comp, const msdp_options* opt,
+                   msdp_stats* out) {
   if (!d || !out) return MSDP_ERR_INVALID_ARGUMENT;
   Solver s;
   if (opt) s.opt = *opt; else msdp_cpu_default_options(&s.opt);
+  if (comp) s.comp = *comp; else msdp_cpu_default_components(&s.comp);
+  const msdp_components& c = s.comp;
+  if (c.algorithm != MSDP_PRIMAL_DUAL || c.schur != MSDP_DENSE_CHOLESKY || c.initial_point != MSDP_SCALED_IDENTITY ||
+      (c.direction != MSDP_NT && c.direction != MSDP_HKM) ||
+      (c.step != MSDP_EIGEN_STEP && c.step != MSDP_CHOLESKY_BACKTRACK) ||
+      (c.centering != MSDP_MEHROTRA && c.centering != MSDP_ADAPTIVE_MU))
+    return MSDP_ERR_UNSUPPORTED;
+  s.nt = c.direction == MSDP_NT;
   if (!load(*d, s)) return MSDP_ERR_INVALID_ARGUMENT;
   const auto t0 = std::chrono::steady_clock::now();
   s.solve();
@@ -797,7 +905,7 @@ int msdp_cpu_solve(const msdp_problem_desc* d, const msdp_options* opt, msdp_sta
 // thread at a time, in order of an atomic counter) until all are done or
 // `seconds` (> 0) have passed; returns how many were solved.
 int msdp_cpu_solve_many(const msdp_problem_desc* problems, int32_t count, int32_t threads, double seconds,
-                        const msdp_options* opt, msdp_stats* out) {
+                        const msdp_components* comp, const msdp_options* opt, msdp_stats* out) {
   if (!problems || !out || count < 0 || threads <= 0) return MSDP_ERR_INVALID_ARGUMENT;
   std::atomic<int> next{0}, done{0};
   const auto t0 = std::chrono::steady_clock::now();
@@ -808,7 +916,7 @@ int msdp_cpu_solve_many(const msdp_problem_desc* problems, int32_t count, int32_
         return;
       const int i = next.fetch_add(1);
       if (i >= count) return;
-      if (msdp_cpu_solve(problems + i, opt, out + i) == MSDP_OK) done.fetch_add(1);
+      if (msdp_cpu_solve(problems + i, comp, opt, out + i) == MSDP_OK) done.fetch_add(1);
       else out[i].status = -1;
     }
   };

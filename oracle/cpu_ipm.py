@@ -1,14 +1,19 @@
 """Build and ctypes binding of the compiled CPU restatement (cpu_ipm.cpp).
 
 TEST INFRASTRUCTURE ONLY, like ``madsdp_oracle``: it times the CPU baseline
-of the batched workloads without interpreter overhead.  It restates the
-default PrimalDual path (NT, EigenStep, Mehrotra, DenseCholesky,
-ScaledIdentity) of MadSDP.jl (src/solver.jl, src/primal_dual.jl,
-src/directions.jl, src/step.jl, src/blocks.jl) following ``madsdp_oracle``
-step by step, and ``tests/test_oracle_cpp.py`` checks it against that module.
+of the batched workloads without interpreter overhead and checks GPU
+results at sizes the NumPy restatement is slow on.  It restates the
+PrimalDual path (NT or HKM, EigenStep or CholeskyBacktrack, Mehrotra or
+AdaptiveMu, with DenseCholesky and ScaledIdentity) of MadSDP.jl
+(src/solver.jl, src/primal_dual.jl, src/directions.jl, src/step.jl,
+src/blocks.jl) following ``madsdp_oracle`` step by step, and
+``tests/test_oracle_cpp.py`` checks it against that module.
 
     build()                         g++ -O3 into oracle/lib/libmsdp_cpu.so
-    solve(model, **options)         one solve, a dict of the stats
+    solve(model, **options)         one solve, a dict of the stats; options:
+                                    direction / step / centering (component
+                                    objects of madsdp_oracle) and the
+                                    options of src/options.jl
     solve_many(models, threads, seconds, **options)
     symeig(A)                       eigenvalues, eigenvectors (test hook)
 """
@@ -56,25 +61,48 @@ def load():
     lib.msdp_cpu_default_options.restype = None
     lib.msdp_cpu_default_options.argtypes = [P(G.Options)]
     lib.msdp_cpu_solve.restype = C.c_int32
-    lib.msdp_cpu_solve.argtypes = [P(G.ProblemDesc), P(G.Options), P(G.Stats)]
+    lib.msdp_cpu_solve.argtypes = [P(G.ProblemDesc), P(G.Components), P(G.Options), P(G.Stats)]
     lib.msdp_cpu_solve_many.restype = C.c_int32
-    lib.msdp_cpu_solve_many.argtypes = [P(G.ProblemDesc), C.c_int32, C.c_int32, C.c_double, P(G.Options),
-                                        P(G.Stats)]
+    lib.msdp_cpu_solve_many.argtypes = [P(G.ProblemDesc), C.c_int32, C.c_int32, C.c_double, P(G.Components),
+                                        P(G.Options), P(G.Stats)]
+    lib.msdp_cpu_default_components.restype = None
+    lib.msdp_cpu_default_components.argtypes = [P(G.Components)]
     lib.msdp_cpu_symeig.restype = C.c_int32
     lib.msdp_cpu_symeig.argtypes = [C.c_int32, P(C.c_double), P(C.c_double), P(C.c_double)]
     _lib = lib
     return lib
 
 
+# component keyword -> (field, value) of msdp_components
+_COMPONENTS = {
+    ("direction", "NT"): ("direction", 0), ("direction", "HKM"): ("direction", 1),
+    ("step", "EigenStep"): ("step", 0), ("step", "CholeskyBacktrack"): ("step", 1),
+    ("centering", "Mehrotra"): ("centering", 0), ("centering", "AdaptiveMu"): ("centering", 1),
+}
+
+
 def _options(lib, options):
+    """(msdp_components, msdp_options) from keywords: direction / step /
+    centering given as component objects of madsdp_oracle (or their class
+    names), the other keywords as options of src/options.jl."""
     from madsdp_gpu import _lib as G
-    o = G.Options()
+    comp, o = G.Components(), G.Options()
+    lib.msdp_cpu_default_components(C.byref(comp))
     lib.msdp_cpu_default_options(C.byref(o))
     for k, v in options.items():
-        if not hasattr(o, k):
+        if k in ("direction", "step", "centering"):
+            name = v if isinstance(v, str) else type(v).__name__
+            if (k, name) not in _COMPONENTS:
+                raise ValueError(f"the compiled restatement has no {k} {name}")
+            setattr(comp, *_COMPONENTS[(k, name)])
+            for field in ("tau", "shrink", "boundary", "sigma_exponent", "initial_ratio", "ratio"):
+                if hasattr(v, field):
+                    setattr(comp, field, getattr(v, field))
+        elif hasattr(o, k):
+            setattr(o, k, v)
+        else:
             raise TypeError(f"unknown option {k}")
-        setattr(o, k, v)
-    return o
+    return comp, o
 
 
 def _stats(s) -> dict:
@@ -86,7 +114,8 @@ def solve(model, **options) -> dict:
     lib = load()
     mm = _Marshalled(model)
     st = _stats_struct()
-    rc = lib.msdp_cpu_solve(C.byref(mm.desc), C.byref(_options(lib, options)), C.byref(st))
+    comp, opts = _options(lib, options)
+    rc = lib.msdp_cpu_solve(C.byref(mm.desc), C.byref(comp), C.byref(opts), C.byref(st))
     if rc != 0:
         raise ValueError(f"msdp_cpu_solve returned {rc}")
     return _stats(st)
@@ -124,7 +153,8 @@ def solve_many(models, threads: int, seconds: float = 0.0, start: int = 0, count
     for i in range(start, start + n):
         prep.stats[i].status = -2
     stats = C.cast(C.byref(prep.stats, start * C.sizeof(prep.stats._type_)), C.POINTER(prep.stats._type_))
-    lib.msdp_cpu_solve_many(prep.marsh.descs(start), n, threads, seconds, C.byref(_options(lib, options)), stats)
+    comp, opts = _options(lib, options)
+    lib.msdp_cpu_solve_many(prep.marsh.descs(start), n, threads, seconds, C.byref(comp), C.byref(opts), stats)
     out = []
     for i in range(start, start + n):
         s = prep.stats[i]

@@ -18,16 +18,20 @@ from problems import build
 KA = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))
 
 
-def agree(model, **options):
+def agree(model, rtol=1e-9, iter_tol=0, **options):
+    """Same status and iterates to rounding (default); with rtol = 1e-7 and
+    iter_tol = 1 the GPU-vs-oracle contract, for runs long and ill-conditioned
+    enough that rounding differences grow to the termination tolerance."""
     c = cpu_ipm.solve(model, **options)
     r = o.Solver(model, **options).solve()
     scale = max(1.0, abs(r.primal_objective()) + abs(r.dual_objective()))
     assert c["status"] == int(r.status)
-    assert c["iter"] == r.iter
-    assert abs(c["pobj"] - r.primal_objective()) <= 1e-9 * scale
-    assert abs(c["dobj"] - r.dual_objective()) <= 1e-9 * scale
-    for key, ref in (("inf_pr", r.inf_pr), ("inf_du", r.inf_du), ("gap", r.inf_compl)):
-        assert abs(c[key] - ref) <= 1e-9 + 1e-3 * ref, key
+    assert abs(c["iter"] - r.iter) <= iter_tol
+    assert abs(c["pobj"] - r.primal_objective()) <= rtol * scale
+    assert abs(c["dobj"] - r.dual_objective()) <= rtol * scale
+    if iter_tol == 0:
+        for key, ref in (("inf_pr", r.inf_pr), ("inf_du", r.inf_du), ("gap", r.inf_compl)):
+            assert abs(c[key] - ref) <= 1e-9 + 1e-3 * ref, key
     return c
 
 
@@ -64,6 +68,38 @@ def test_dense_mixed_cones():
 def test_dense_one_block_served_mix_shape():
     from madsdp_gpu.serving import _dense_request
     agree(_dense_request(np.random.default_rng(7), 16, 16, 60, 11))
+
+
+COMBOS = [(d, st, c) for d in ("NT", "HKM") for st in ("EigenStep", "CholeskyBacktrack")
+          for c in ("Mehrotra", "AdaptiveMu")]
+
+
+@pytest.mark.parametrize("direction,step,centering", COMBOS)
+def test_component_matrix(direction, step, centering):
+    """The reference's component matrix (test/runtests.jl:157-184) and an
+    SOS and a max-cut instance with every combination."""
+    comps = dict(direction=getattr(o, direction)(), step=getattr(o, step)(), centering=getattr(o, centering)())
+    cm = KA["component_matrix"]
+    for model, expected in cm["problems"]:
+        c = agree(build(model), max_iter=cm["max_iter"], **comps)
+        assert c["status"] == 1 and abs(c["pobj"] - expected) <= cm["atol"]
+    # SOS under AdaptiveMu: 33 iterations, cond(X) and cond(S) reach 4.5e12
+    # (1e9-1e10 under Mehrotra), ending at the tolerance edge
+    loose = dict(rtol=1e-7, iter_tol=1) if centering == "AdaptiveMu" else {}
+    agree(g.sos_hankel(11, seed=2), **loose, **comps)
+    agree(g.maxcut(16, 0.3, seed=5), **comps)
+
+
+def test_component_parameters():
+    """Non-default constants reach the compiled restatement."""
+    agree(g.sos_hankel(8, seed=3), step=o.EigenStep(tau=0.9), centering=o.Mehrotra(sigma_exponent=2.0))
+    agree(g.sos_hankel(8, seed=3), rtol=1e-7, iter_tol=1, step=o.CholeskyBacktrack(shrink=0.5, boundary=0.9),
+          centering=o.AdaptiveMu(initial_ratio=0.5, ratio=0.3))
+
+
+def test_unsupported_component_rejected():
+    with pytest.raises(ValueError):
+        cpu_ipm.solve(build("trivial_2x2"), direction="XYZ")
 
 
 def test_max_iter_status():
