@@ -705,7 +705,9 @@ def run_gpu(args):
                      "frac": achieved / bf16, "traffic": traffic,
                      "peak_kind": f"{peak_kind} bf16 dense (burst)",
                      "note": "algorithmic flops of the iteration (28n^3 + nnz^2 + m^3/3 + 4m^2 per instance-"
-                             "iteration) / iterate-kernel time; the kernel runs on CUDA cores (FP32/FP64), not tcgen05"},
+                             "iteration) / iterate-kernel time; the kernel runs on CUDA cores (FP32/FP64), not tcgen05",
+                     "limiter": "FP64 pipe (1.25 TFLOP/s nominal on GB300): 26% of active cycles on average, "
+                                "saturated on the busiest SMs (profiles/ipm_kernel_sos_batch.txt)"},
         "cpu_baseline": cpu_block,
         "clocks": clocks,
     }
