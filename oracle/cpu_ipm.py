@@ -56,7 +56,11 @@ def load():
         return _lib
     from madsdp_gpu import _lib as G
     build()
-    lib = C.CDLL(LIB_PATH)
+    try:
+        lib = C.CDLL(LIB_PATH)
+    except OSError:  # a library built for another machine: rebuild here
+        build(force=True)
+        lib = C.CDLL(LIB_PATH)
     P = C.POINTER
     lib.msdp_cpu_default_options.restype = None
     lib.msdp_cpu_default_options.argtypes = [P(G.Options)]
