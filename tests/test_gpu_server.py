@@ -118,3 +118,30 @@ def test_serve_poisson_stream(gpu_ctx):
     assert out["completed"] == out["requests"] == len(stream) > 0
     assert out["succeeded"] == out["completed"]
     assert out["p99_latency_ms"] >= out["p50_latency_ms"] > 0
+
+
+@pytest.mark.parametrize("precision,rtol", [("fp64", 1e-7), ("mixed", 5e-7)])
+def test_served_mix_matches_oracle(gpu_ctx, precision, rtol):
+    """Every request of a served Poisson stream with the benchmark's mix
+    (SOS d <= 127, max-cut n <= 100, dense n <= 32 with m <= 200) converges
+    and agrees with the compiled oracle: objectives within
+    rtol * max(1, |p| + |d|) (the FP64 and mixed tolerances of the batch
+    parity tests)."""
+    import os
+
+    import bench
+    from oracle import cpu_ipm
+    stream = poisson_stream(40.0, 1.5, seed=23, **bench.SERVE_MIX)
+    models = [m for _, _, m in stream]
+    ref = cpu_ipm.solve_many(models, threads=os.cpu_count() or 1)
+    srv = Server(memory_budget_bytes=2 << 30, max_slots=256, precision=precision)
+    ids = [srv.submit(m) for m in models]
+    srv.drain(50)
+    kinds = [k for _, k, _ in stream]
+    for rid, kind, r in zip(ids, kinds, ref):
+        s = srv.result(rid)
+        assert r["status"] == 1
+        assert s["status"] == M.Status.SOLVE_SUCCEEDED, (rid, kind, s["status"])
+        scale = max(1.0, abs(r["pobj"]) + abs(r["dobj"]))
+        assert abs(s["pobj"] - r["pobj"]) <= rtol * scale, (rid, kind, s["pobj"], r["pobj"])
+    srv.close()
