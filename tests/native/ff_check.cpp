@@ -1,0 +1,72 @@
+// CPU test harness of the float-float arithmetic (csrc/ff.cuh): element-wise
+// operations, the error-free transformations, a dot product and a
+// Cholesky factorization carried out in float-float.
+#include <cstdint>
+
+#include "../../madsdp.jl_gb300/csrc/ff.cuh"
+
+extern "C" {
+
+// 1 where hi + lo equals the exact sum (op 0) or product (op 1) of the
+// FP32 inputs (both exact in float64 for these operations)
+void ff_eft_check(int op, int64_t n, const float* a, const float* b, int32_t* ok) {
+  for (int64_t i = 0; i < n; ++i) {
+    const ff r = op == 0 ? ff_two_sum(a[i], b[i]) : ff_two_prod(a[i], b[i]);
+    const double exact = op == 0 ? (double)a[i] + (double)b[i] : (double)a[i] * (double)b[i];
+    ok[i] = ((double)r.hi + (double)r.lo) == exact;
+  }
+}
+
+// op: 0 add, 1 sub, 2 mul, 3 div, 4 sqrt(a), 5 fma (a * b + a); inputs are
+// rounded to float-float first (ain / bin return those values)
+void ff_elementwise(int op, int64_t n, const double* a, const double* b, double* ain, double* bin, double* out) {
+  for (int64_t i = 0; i < n; ++i) {
+    const ff x = ff_from_double(a[i]), y = ff_from_double(b[i]);
+    ain[i] = ff_to_double(x);
+    bin[i] = ff_to_double(y);
+    ff r{};
+    switch (op) {
+      case 0: r = ff_add(x, y); break;
+      case 1: r = ff_sub(x, y); break;
+      case 2: r = ff_mul(x, y); break;
+      case 3: r = ff_div(x, y); break;
+      case 4: r = ff_sqrt(x); break;
+      default: r = ff_fma(x, y, x); break;
+    }
+    out[i] = ff_to_double(r);
+  }
+}
+
+double ff_dot(int64_t n, const double* x, const double* y) {
+  ff s = ff_from(0.0f);
+  for (int64_t i = 0; i < n; ++i) s = ff_fma(ff_from_double(x[i]), ff_from_double(y[i]), s);
+  return ff_to_double(s);
+}
+
+// Lower Cholesky factor of the column-major n x n A in float-float
+// (left-looking); returns 0 at a non-positive pivot.
+int ff_cholesky(int n, const double* A, double* L) {
+  ff* l = new ff[(size_t)n * n];
+  int ok = 1;
+  for (int j = 0; j < n && ok; ++j) {
+    ff d = ff_from_double(A[(size_t)j + (size_t)j * n]);
+    for (int p = 0; p < j; ++p) d = ff_sub(d, ff_mul(l[j + (size_t)p * n], l[j + (size_t)p * n]));
+    if (!(d.hi > 0.0f)) {
+      ok = 0;
+      break;
+    }
+    const ff djj = ff_sqrt(d);
+    l[j + (size_t)j * n] = djj;
+    for (int i = j + 1; i < n; ++i) {
+      ff s = ff_from_double(A[(size_t)i + (size_t)j * n]);
+      for (int p = 0; p < j; ++p) s = ff_sub(s, ff_mul(l[i + (size_t)p * n], l[j + (size_t)p * n]));
+      l[i + (size_t)j * n] = ff_div(s, djj);
+    }
+  }
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) L[(size_t)i + (size_t)j * n] = i >= j && ok ? ff_to_double(l[i + (size_t)j * n]) : 0.0;
+  delete[] l;
+  return ok;
+}
+
+}  // extern "C"
