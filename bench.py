@@ -363,12 +363,15 @@ def run_instance(args):
     stream = torch.cuda.ExternalStream(ctx.stream_handle, device=torch.device("cuda", 0))
     # the engine MadSDPSolver(model) picks: one thread block (a one-problem
     # batch) for small problems, the whole-GPU solver for large ones
-    engine = "instance" if (args.precision == "fp64_tensor" or M.solver._use_instance_engine(model)) else "batch"
+    if args.precision == "mixed":
+        engine = "batch"
+    else:
+        engine = "instance" if (args.precision == "fp64_tensor" or M.solver._use_instance_engine(model)) else "batch"
     if engine == "instance":
         solver = M.InstanceSolver(model, context=ctx, precision=args.precision)
         run = solver.solve
     else:
-        solver = M.Batch([model], context=ctx)
+        solver = M.Batch([model], context=ctx, precision="mixed" if args.precision == "mixed" else "fp64")
         run = solver.solve
     for _ in range(args.warmup):
         run()
@@ -420,7 +423,8 @@ def run_instance(args):
     line = {
         "metric": METRIC, "value": 1.0 / t_solve, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(ms), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64 (tensor-core emulated products)",
+        "vs_baseline": None, "dtype": {"fp64": "f64", "fp64_tensor": "f64 (tensor-core emulated products)",
+                  "mixed": "f32+f64"}[args.precision],
         "data": "synthetic",
         "config": {"workload": args.workload, "precision": args.precision, **{k: v for k, v in spec.items() if k != "kind"}, "seed": args.seed,
                    "m": model.m, "components": "PrimalDual(NT, EigenStep, Mehrotra) + DenseCholesky, ScaledIdentity",
@@ -731,8 +735,9 @@ def main():
     ap.add_argument("--serve-iterations", type=int, default=1000)
     ap.add_argument("--serve-budget-ms", type=float, default=20.0)
     ap.add_argument("--workload", default="sos_batch", choices=["sos_batch", *INSTANCE_WORKLOADS])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_tensor"],
-                    help="instance workloads: FP64, or FP64 products emulated on tensor cores")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_tensor", "mixed"],
+                    help="instance workloads: FP64, FP64 products emulated on tensor cores (whole-GPU engine), "
+                         "or mixed precision in one thread block (the batch engine)")
     args = ap.parse_args()
     if args.workload != "sos_batch":
         if args.impl == "reference":
