@@ -20,6 +20,7 @@
 
 #include "../../include/madsdp_gpu.h"
 #include "launch.h"
+#include "freelist.h"
 #include "stage.h"
 
 struct msdp_context;  // defined in capi.cu; a server runs on its own streams
@@ -196,38 +197,6 @@ struct msdp_server {
 };
 
 namespace {
-
-// first-fit allocation from a free list (offset -> size)
-int64_t list_alloc(std::map<int64_t, int64_t>& fl, int64_t size) {
-  if (size <= 0) return 0;
-  for (auto it = fl.begin(); it != fl.end(); ++it) {
-    if (it->second >= size) {
-      const int64_t off = it->first;
-      const int64_t rest = it->second - size;
-      fl.erase(it);
-      if (rest > 0) fl[off + size] = rest;
-      return off;
-    }
-  }
-  return -1;
-}
-
-void list_free(std::map<int64_t, int64_t>& fl, int64_t off, int64_t size) {
-  if (size <= 0) return;
-  auto it = fl.emplace(off, size).first;
-  auto next = std::next(it);
-  if (next != fl.end() && it->first + it->second == next->first) {
-    it->second += next->second;
-    fl.erase(next);
-  }
-  if (it != fl.begin()) {
-    auto prev = std::prev(it);
-    if (prev->first + prev->second == it->first) {
-      prev->second += it->second;
-      fl.erase(it);
-    }
-  }
-}
 
 BatchDev server_dev(msdp_server* s, const Wave& w, const int32_t* order, int count) {
   BatchDev B;
