@@ -853,7 +853,7 @@ void msdp_cpu_default_options(msdp_options* o) {
 
 // The defaults of src/components.jl (PrimalDual, NT, EigenStep(0.95),
 // Mehrotra(3), ScaledIdentity(), DenseCholesky; CholeskyBacktrack(0.8,
-// 0.95), AdaptiveMu(1/4, 1/2)).
+// 0.95), AdaptiveMu(1/4, 1/2), DualShift(1, 1e10), DualCentering(0.2, 1, 2)).
 void msdp_cpu_default_components(msdp_components* c) {
   std::memset(c, 0, sizeof(*c));
   c->algorithm = MSDP_PRIMAL_DUAL;
@@ -871,6 +871,11 @@ void msdp_cpu_default_components(msdp_components* c) {
   c->initial_ratio = 0.25;
   c->ratio = 0.5;
   c->scale = 0.0;
+  c->initial_shift = 1.0;  // DualShift and DualCentering: not run here, kept equal to the library's
+  c->max_shift = 1e10;
+  c->dc_beta = 0.2;
+  c->dc_delta = 1.0;
+  c->dc_A = 2.0;
 }
 
 // One solve with `comp` and `opt` (the defaults when null); writes status,

@@ -153,3 +153,20 @@ def test_symeig(kind):
     assert np.max(np.abs(w - np.linalg.eigvalsh(A))) <= 1e-12 * scale * k
     assert np.max(np.abs(V.T @ V - np.eye(k))) <= 1e-12 * k
     assert np.max(np.abs(V @ np.diag(w) @ V.T - A)) <= 1e-12 * scale * k
+
+
+def test_defaults_equal_the_gpu_library_defaults():
+    """The compiled restatement starts from the same components and options
+    as the GPU library (both mirror src/components.jl and src/options.jl)."""
+    import ctypes as C
+
+    from madsdp_gpu import _lib as G
+    gpu, cpu = G.load(), cpu_ipm.load()
+    for struct, gfun, cfun in ((G.Components, gpu.msdp_default_components, cpu.msdp_cpu_default_components),
+                               (G.Options, gpu.msdp_default_options, cpu.msdp_cpu_default_options)):
+        a, b = struct(), struct()
+        gfun(C.byref(a))
+        cfun(C.byref(b))
+        for name, _ in struct._fields_:
+            va, vb = getattr(a, name), getattr(b, name)
+            assert va == vb or (va != va and vb != vb), (struct.__name__, name, va, vb)
