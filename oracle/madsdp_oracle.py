@@ -183,6 +183,7 @@ class _BlockOp:
         self.P = sp.csr_matrix((np.ones(self.nnz), (self.con, np.arange(self.nnz))), shape=(m, self.nnz))
         self.ptr = np.asarray(blk.ptr)
         self.dense_threshold = 6000
+        self._dense = None
 
     def jprod(self, X):
         return self.sp @ X.ravel()
@@ -197,12 +198,28 @@ class _BlockOp:
         return A
 
     def schur(self, L, R):
-        """H_jk = <A_j, L A_k R>."""
+        """H_jk = <A_j, L A_k R>: entry pairs for few entries, batched dense
+        products when the constraints are dense, else constraint by
+        constraint (three summation orders of the same sum)."""
         if self.nnz <= self.dense_threshold:
             r, c, v = self.row, self.col, self.val
             # K[e, f] = v_e v_f L[r_e, r_f] R[c_f, c_e];  H = P K P'
             K = (v[:, None] * v[None, :]) * L[np.ix_(r, r)] * R[np.ix_(c, c)].T
             return np.asarray(self.P @ np.asarray(self.P @ K.T).T)
+        if 2 * self.nnz >= self.m * self.n * self.n:
+            return self.schur_dense(L, R)
+        return self.schur_columns(L, R)
+
+    def schur_dense(self, L, R):
+        """All T_k = L A_k R by batched products, then H = [vec A_j]' [vec T_k]
+        as one product: 4 m n^3 + 2 m^2 n^2 flops on dense A_k."""
+        if self._dense is None:
+            self._dense = self.sp.toarray().reshape(self.m, self.n, self.n)
+        T = np.matmul(np.matmul(L, self._dense), R)
+        return self._dense.reshape(self.m, -1) @ T.reshape(self.m, -1).T
+
+    def schur_columns(self, L, R):
+        """T_k = L A_k R from the entries of A_k, H[:, k] = A(T_k)."""
         H = np.zeros((self.m, self.m))
         for k in range(self.m):
             s, e = self.ptr[k], self.ptr[k + 1]

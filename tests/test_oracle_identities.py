@@ -48,3 +48,25 @@ def test_newton_identities_dense_vs_qr(scalars, diagonal):
         assert np.allclose(a.delx, c.delx, atol=1e-10)
         assert np.allclose(a.delz, c.delz, atol=1e-10)
         assert np.allclose(a.blocks[0].delX, c.blocks[0].delX, atol=1e-10)
+
+
+@pytest.mark.parametrize("sides,m", [([6], 20), ([12], 60), ([9, 5], 40), ([16], 100)])
+def test_dense_schur_summation_orders_agree(sides, m):
+    """The oracle's three summation orders of H_jk = <A_j, L A_k R> (entry
+    pairs, constraint by constraint, batched dense products) agree on
+    dense constraints, for symmetric L = R (NT) and L != R (HKM)."""
+    from oracle.madsdp_oracle import _BlockOp
+    model = g.dense_random(sides, 0, m, seed=7)
+    rng = np.random.default_rng(1)
+    for blk in model.A:
+        op = _BlockOp(blk)
+        n = op.n
+        M1, M2 = rng.standard_normal((n, n)), rng.standard_normal((n, n))
+        W = M1 @ M1.T + n * np.eye(n)
+        X, Si = M2 @ M2.T + n * np.eye(n), W / n
+        for L, R in ((W, W), (Si, X)):
+            ref = op.schur_columns(L, R)
+            scale = np.abs(ref).max()
+            assert np.abs(op.schur_dense(L, R) - ref).max() <= 1e-13 * scale
+            if op.nnz <= op.dense_threshold:  # the entry-pair order (nnz^2 memory)
+                assert np.abs(op.schur(L, R) - ref).max() <= 1e-13 * scale
