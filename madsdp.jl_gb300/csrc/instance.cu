@@ -101,7 +101,8 @@ __global__ void k_reduce_final(int op, int np, const double* __restrict__ partia
 }
 
 // out = a*A + b*B + c*C + d*D + e*E, left to right; absent terms skipped.
-__global__ void k_lin(int64_t N, double* __restrict__ out, double a, const double* A, double b, const double* B,
+// out may be one of the inputs (in-place updates such as X += a dX): no __restrict__
+__global__ void k_lin(int64_t N, double* out, double a, const double* A, double b, const double* B,
                       double c, const double* Cc, double d, const double* D, double e, const double* E) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     double v = a * A[i];
