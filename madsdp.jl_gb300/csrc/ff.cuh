@@ -114,3 +114,23 @@ FF_HD ff ff_from_double(double v) {
   return {hi, (float)(v - (double)hi)};
 }
 FF_HD double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+
+// Operators, so that the templated CTA routines (products, Cholesky) can be
+// instantiated with T = ff.  Comparisons order by hi, then lo (exact for
+// normalized values).
+FF_HD ff operator+(ff a, ff b) { return ff_add(a, b); }
+FF_HD ff operator-(ff a, ff b) { return ff_sub(a, b); }
+FF_HD ff operator-(ff a) { return ff_neg(a); }
+FF_HD ff operator*(ff a, ff b) { return ff_mul(a, b); }
+FF_HD ff operator/(ff a, ff b) { return ff_div(a, b); }
+FF_HD ff& operator+=(ff& a, ff b) { return a = ff_add(a, b); }
+FF_HD ff& operator-=(ff& a, ff b) { return a = ff_sub(a, b); }
+FF_HD ff& operator*=(ff& a, ff b) { return a = ff_mul(a, b); }
+FF_HD bool operator<(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+FF_HD bool operator>(ff a, ff b) { return b < a; }
+FF_HD bool operator<=(ff a, ff b) { return !(b < a); }
+FF_HD bool operator>=(ff a, ff b) { return !(a < b); }
+FF_HD bool operator==(ff a, ff b) { return a.hi == b.hi && a.lo == b.lo; }
+FF_HD bool operator!=(ff a, ff b) { return !(a == b); }
+FF_HD ff sqrt(ff a) { return ff_sqrt(a); }
+FF_HD ff fabs(ff a) { return a.hi < 0.0f || (a.hi == 0.0f && a.lo < 0.0f) ? ff_neg(a) : a; }

@@ -70,3 +70,29 @@ int ff_cholesky(int n, const double* A, double* L) {
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// the operators on pairs (a_i, b_i): out[6 i + k] for k = + - * / sqrt(|a|) fabs(a);
+// cmp[4 i + k] for k = < > <= ==
+void ff_operators(int64_t n, const double* a, const double* b, double* out, int32_t* cmp) {
+  for (int64_t i = 0; i < n; ++i) {
+    const ff x = ff_from_double(a[i]), y = ff_from_double(b[i]);
+    out[6 * i + 0] = ff_to_double(x + y);
+    out[6 * i + 1] = ff_to_double(x - y);
+    out[6 * i + 2] = ff_to_double(x * y);
+    out[6 * i + 3] = ff_to_double(x / y);
+    out[6 * i + 4] = ff_to_double(sqrt(fabs(x)));
+    out[6 * i + 5] = ff_to_double(fabs(x));
+    ff z = x;
+    z += y;
+    z -= y;  // x + y - y, to check the compound forms run the same code
+    (void)z;
+    cmp[4 * i + 0] = x < y;
+    cmp[4 * i + 1] = x > y;
+    cmp[4 * i + 2] = x <= y;
+    cmp[4 * i + 3] = x == y;
+  }
+}
+
+}  // extern "C"

@@ -100,3 +100,24 @@ def test_cholesky_rejects_indefinite(lib):
     M = np.asfortranarray(np.diag([1.0, -1e-3, 2.0]))
     L = np.zeros((3, 3), order="F")
     assert lib.ff_cholesky(3, M.ctypes.data_as(D), L.ctypes.data_as(D)) == 0
+
+
+def test_operators_match_the_functions_and_order(lib):
+    """The operator forms give the named operations' results, and the
+    comparisons order float-float values as float64 orders their sums."""
+    lib.ff_operators.argtypes = [C.c_int64, D, D, D, C.POINTER(C.c_int32)]
+    rng = np.random.default_rng(8)
+    a = values(rng, 5000)
+    b = np.where(rng.random(5000) < 0.1, a, values(rng, 5000))  # some equal pairs
+    out = np.zeros(6 * a.size)
+    cmp = np.zeros(4 * a.size, np.int32)
+    lib.ff_operators(a.size, a.ctypes.data_as(D), b.ctypes.data_as(D), out.ctypes.data_as(D),
+                     cmp.ctypes.data_as(C.POINTER(C.c_int32)))
+    out, cmp = out.reshape(-1, 6), cmp.reshape(-1, 4)
+    ain, bin_, _ = elementwise(lib, 0, a, b)
+    for op, col in ((0, 0), (1, 1), (2, 2), (3, 3)):
+        assert np.array_equal(out[:, col], elementwise(lib, op, a, b)[2])
+    assert np.array_equal(out[:, 5], np.abs(ain))
+    assert np.max(np.abs(out[:, 4] - np.sqrt(np.abs(ain))) / np.sqrt(np.abs(ain))) <= 2.0 ** -44
+    assert np.array_equal(cmp[:, 0], ain < bin_) and np.array_equal(cmp[:, 1], ain > bin_)
+    assert np.array_equal(cmp[:, 2], ain <= bin_) and np.array_equal(cmp[:, 3], ain == bin_)
