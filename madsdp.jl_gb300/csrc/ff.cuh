@@ -28,6 +28,13 @@
 
 struct ff {
   float hi, lo;
+  ff() = default;
+  FF_HD constexpr ff(float h, float l) : hi(h), lo(l) {}
+  // from a number: rounded to the nearest float-float (for double, hi is
+  // the nearest float and lo the nearest float to the remainder)
+  FF_HD explicit ff(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+  FF_HD explicit ff(float v) : hi(v), lo(0.0f) {}
+  FF_HD explicit ff(int v) : ff((double)v) {}
 };
 
 FF_HD float ff_fmaf(float a, float b, float c) {
@@ -133,4 +140,5 @@ FF_HD bool operator>=(ff a, ff b) { return !(a < b); }
 FF_HD bool operator==(ff a, ff b) { return a.hi == b.hi && a.lo == b.lo; }
 FF_HD bool operator!=(ff a, ff b) { return !(a == b); }
 FF_HD ff sqrt(ff a) { return ff_sqrt(a); }
+FF_HD ff fma(ff a, ff b, ff c) { return ff_fma(a, b, c); }  // a * b + c
 FF_HD ff fabs(ff a) { return a.hi < 0.0f || (a.hi == 0.0f && a.lo < 0.0f) ? ff_neg(a) : a; }

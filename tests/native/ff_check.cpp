@@ -96,3 +96,24 @@ void ff_operators(int64_t n, const double* a, const double* b, double* out, int3
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// conversions: ff(double), ff(int), (ff)0 and fma(a, b, c) against the named functions
+int ff_constructors(int64_t n, const double* a, const double* b, const double* c) {
+  for (int64_t i = 0; i < n; ++i) {
+    const ff x(a[i]), y(b[i]), z(c[i]);
+    const ff f = ff_from_double(a[i]);
+    if (x.hi != f.hi || x.lo != f.lo) return 1;
+    const ff r = fma(x, y, z), q = ff_fma(x, y, z);
+    if (r.hi != q.hi || r.lo != q.lo) return 2;
+  }
+  const ff zero = (ff)0, one = (ff)1, big(123456789);
+  if (zero.hi != 0.0f || zero.lo != 0.0f || one.hi != 1.0f || one.lo != 0.0f) return 3;
+  if (ff_to_double(big) != 123456789.0) return 4;  // 27 bits: exact in float-float
+  ff v{};
+  if (v.hi != 0.0f || v.lo != 0.0f) return 5;  // value-initialized
+  return 0;
+}
+
+}  // extern "C"

@@ -121,3 +121,11 @@ def test_operators_match_the_functions_and_order(lib):
     assert np.max(np.abs(out[:, 4] - np.sqrt(np.abs(ain))) / np.sqrt(np.abs(ain))) <= 2.0 ** -44
     assert np.array_equal(cmp[:, 0], ain < bin_) and np.array_equal(cmp[:, 1], ain > bin_)
     assert np.array_equal(cmp[:, 2], ain <= bin_) and np.array_equal(cmp[:, 3], ain == bin_)
+
+
+def test_constructors_and_fma(lib):
+    lib.ff_constructors.argtypes = [C.c_int64, D, D, D]
+    lib.ff_constructors.restype = C.c_int
+    rng = np.random.default_rng(9)
+    a, b, c = values(rng, 2000), values(rng, 2000), values(rng, 2000)
+    assert lib.ff_constructors(a.size, a.ctypes.data_as(D), b.ctypes.data_as(D), c.ctypes.data_as(D)) == 0
