@@ -187,7 +187,9 @@ def cpu_batch_block(cpu, args, gpu_stats):
 
 
 CPU_PORT = "compiled C++ restatement of the oracle (oracle/cpu_ipm.cpp: FP64, NT+EigenStep+Mehrotra+DenseCholesky, " \
-           "own dense kernels, no BLAS)"
+           "own dense kernels, no BLAS; its Hankel Schur assembly is the entry-pair sum, about n^4 per iteration, " \
+           "while the GPU's FP64 path assembles by FFT along one index, O(n^3 log n): part of the ratio is that " \
+           "algorithmic difference)"
 
 
 # ----------------------------------------------------------------- single large instances
@@ -408,7 +410,7 @@ def run_instance(args):
     e2.close()
     t_solve = statistics.mean(ms) / 1000.0
     flops = instance_flops_per_iteration(model) * st["iter"]
-    fp64_peak = 1.25e3  # GB300 FP64 nominal, GFLOP/s
+    fp64_peak, _ = measured_fp_rates()  # GFLOP/s
     cpu_block = port_block(*port) if port is not None else None
     if cpu is not None:
         per_it, nit, init = cpu
@@ -437,7 +439,7 @@ def run_instance(args):
         "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "fp64", "achieved": flops / t_solve / 1e9, "peak": fp64_peak, "unit": "GFLOP/s",
                      "frac": flops / t_solve / 1e9 / fp64_peak, "traffic": None,
-                     "peak_kind": "nominal FP64 dense (no measured FP64 peak)",
+                     "peak_kind": "measured FP64 FMA throughput (profiles/gb300_primitives.txt)",
                      "note": "algorithmic flops of the iterations (model above) / solve time"},
         "cpu_baseline": cpu_block,
         "clocks": clocks,
@@ -495,6 +497,25 @@ class ClockSampler:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def measured_fp_rates():
+    """(FP64, FP32) CUDA-core rates in GFLOP/s measured on GB300
+    (profiles/gb300_primitives.txt: FMA throughput of independent chains)."""
+    fp64, fp32 = 1000.0, 67000.0
+    p = os.path.join(ROOT, "profiles", "gb300_primitives.txt")
+    if os.path.exists(p):
+        for line in open(p):
+            if "TFLOP/s" in line and line.startswith(("fp64 fma throughput", "fp32 fma throughput")):
+                try:
+                    v = float(line.split("~")[1].split("TFLOP/s")[0]) * 1e3
+                except (IndexError, ValueError):
+                    continue
+                if line.startswith("fp64"):
+                    fp64 = v
+                else:
+                    fp32 = v
+    return fp64, fp32
 
 
 def measured_peaks():
@@ -578,7 +599,12 @@ def run_gpu(args):
     __graft_entry__.build()
     import madsdp_gpu as M
 
-    models, ds = workload(args.instances, args.seed + rank)
+    # every rank draws the same world x instances problems and takes its
+    # cost-balanced share (weak scaling: `instances` per GPU on average)
+    from madsdp_gpu.distributed import shard_by_cost, solve_cost
+    all_models, all_ds = workload(args.instances * world, args.seed)
+    mine = shard_by_cost([solve_cost(mm) for mm in all_models], world)[rank] if world > 1 else list(range(len(all_models)))
+    models, ds = [all_models[i] for i in mine], [all_ds[i] for i in mine]
     ctx = M.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream_handle, device=torch.device("cuda", local))
 
@@ -629,9 +655,10 @@ def run_gpu(args):
     from madsdp_gpu.distributed import max_over_ranks
     total_ms = max_over_ranks(sum(step_ms))
     value = args.instances * world * args.steps / (total_ms / 1000.0)
-    fp64_value = args.instances / (statistics.mean(s64) / 1000.0)
+    fp64_value = len(models) / (statistics.mean(s64) / 1000.0)
 
-    # ---- end to end through the public API with host buffers
+    # ---- end to end through the public API with host buffers: upload,
+    # solve, every instance's statistics and solution (X, y, x, z) back
     e2e_times = []
     h2d = d2h = 0
     for k in range(args.e2e_steps):
@@ -640,11 +667,12 @@ def run_gpu(args):
         be = M.Batch(models, precision="mixed", context=ctx)
         be.launch_solve()
         st = be.all_stats()
+        sols = be.all_solutions()
         h2d = be.upload_bytes
-        d2h = len(st) * 120
+        d2h = len(st) * 120 + 8 * sum(sum(x.size for x in X) + y.size + xx.size + z.size for X, y, xx, z in sols)
         be.close()
         e2e_times.append(time.perf_counter() - t0)
-    e2e_value = args.instances / statistics.mean(e2e_times[1:] if len(e2e_times) > 1 else e2e_times)
+    e2e_value = len(models) / statistics.mean(e2e_times[1:] if len(e2e_times) > 1 else e2e_times)
 
     # ---- served Poisson stream (continuous batching, real time)
     serving = None
@@ -679,6 +707,7 @@ def run_gpu(args):
         flops += s["iter"] * flops_per_iteration(n, mdl.m, mdl.A[0].nnz)
     kern_s = statistics.mean(kern_ms) / 1000.0
     hbm, bf16, peak_kind = measured_peaks()
+    fp64_rate, fp32_rate = measured_fp_rates()
     achieved = flops / kern_s / 1e12
     traffic = profiled_traffic()
     cpu_block, oracle_err = cpu_batch_block(cpu, args, stm)
@@ -688,6 +717,7 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {
             "workload": "sos_hankel_batch (4th workload: batched SOS SDPs)", "instances_per_gpu": args.instances,
+            "instances_this_rank": len(models),
             "d_range": [5, 63], "m": "2d+1", "ns": 2, "seed": args.seed,
             "components": "PrimalDual(NT, EigenStep, Mehrotra) + DenseCholesky, ScaledIdentity",
             "precision": "mixed: FP32 block algebra and Schur factor, each direction refined twice against the "
@@ -711,7 +741,10 @@ def run_gpu(args):
                      "note": "algorithmic flops of the iteration (28n^3 + nnz^2 + m^3/3 + 4m^2 per instance-"
                              "iteration) / iterate-kernel time; the kernel runs on CUDA cores (FP32/FP64), not tcgen05",
                      "limiter": "FP64 pipe (1.25 TFLOP/s nominal on GB300): 26% of active cycles on average, "
-                                "saturated on the busiest SMs (profiles/ipm_kernel_sos_batch.txt)"},
+                                "saturated on the busiest SMs (profiles/ipm_kernel_sos_batch.txt)",
+                     "fp64_pipe_frac": achieved * 1e3 / fp64_rate, "fp32_pipe_frac": achieved * 1e3 / fp32_rate,
+                     "pipe_peaks_gflops": {"fp64": fp64_rate, "fp32": fp32_rate,
+                                           "source": "measured FMA throughput, profiles/gb300_primitives.txt"}},
         "cpu_baseline": cpu_block,
         "clocks": clocks,
     }

@@ -188,6 +188,12 @@ int msdp_batch_get_all_stats(msdp_batch* batch, msdp_stats* out /* [nprob] */);
 /* X per block (n_i*n_i each), y (m), x (ns), z (ns); NULL pointers are skipped. */
 int msdp_batch_get_solution(msdp_batch* batch, int32_t prob, double* const* X, double* y,
                             double* x, double* z);
+/* Every problem's solution in one download: for each problem in order, X of
+ * each block (column-major n x n), then y (m), x (ns) and z (ns), packed into
+ * `out` of msdp_batch_solution_size() doubles (MOI.get(::Solver,
+ * ::LRO.Solution), src/moi.jl:76-78, for a whole batch). */
+int64_t msdp_batch_solution_size(const msdp_batch* batch);
+int msdp_batch_get_all_solutions(msdp_batch* batch, double* out);
 int msdp_batch_get_trajectory(msdp_batch* batch, int32_t prob, msdp_iter_record* out,
                               int32_t capacity, int32_t* count);
 
@@ -314,6 +320,34 @@ const char* msdp_solver_profile_field_name(int32_t index);
 /* Launches of this library's own kernels (library calls not counted). */
 int64_t msdp_solver_launch_count(const msdp_solver* solver);
 const char* msdp_solver_last_error(const msdp_solver* solver);
+
+/* ---- split-precision products on the tensor cores ---------------------------
+ * C = alpha op(A) op(B) + beta C for column-major float64 device arrays
+ * (op = transpose when trans != 0), computed from bf16 slices of A and B on
+ * the tcgen05 tensor cores with exact per-chunk accumulation:
+ *   precision MSDP_FP64   7 slices, 28 slice products: error about 2e-14 of
+ *                         |op(A)||op(B)| (the dense products of the FP64
+ *                         whole-GPU path);
+ *   precision MSDP_MIXED  3 slices, 6 slice products: about FP32 accuracy
+ *                         (the split-precision Schur assembly).
+ * lower != 0 (M == N) computes only the entries with row >= column.  This
+ * is the dense contraction behind LowRankOpt's schur_complement! for dense
+ * constraints (called at src/solver.jl:304) and the products of
+ * src/directions.jl:45-100; the entry point allocates its slice buffers per
+ * call and synchronizes `stream` (a cudaStream_t, NULL = default). */
+int msdp_tc_gemm(int32_t precision, int32_t transa, int32_t transb, int64_t M, int64_t N, int64_t K, double alpha,
+                 const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                 int32_t lower, void* stream);
+
+/* DenseCholesky's factorize! (src/schur_solvers.jl:15-19, cholesky! with
+ * issuccess) for one dense n x n column-major float64 device matrix: the
+ * lower factor overwrites the lower triangle (the strict upper triangle is
+ * not touched).  *info = k + 1 for the first pivot k that is not positive
+ * and finite, else 0 (LAPACK potrf).  Blocked right-looking factorization
+ * whose trailing updates are tensor-core products as in msdp_tc_gemm;
+ * MSDP_MIXED gives an FP32-class factor (the refinement-based Schur solve).
+ * Allocates its workspace per call and synchronizes `stream`. */
+int msdp_dense_cholesky(int32_t precision, int32_t n, double* A, int64_t lda, int32_t* info, void* stream);
 
 #ifdef __cplusplus
 }

@@ -47,6 +47,10 @@ struct msdp_batch {
   int64_t launches = 0;
   int64_t upload_bytes = 0;
   int grid = 0;
+  // packed download of every solution (built on the first call)
+  double* gsol = nullptr;
+  void* gseg = nullptr;
+  int64_t nseg = 0, sol_size = 0;
 };
 
 namespace {
@@ -155,7 +159,7 @@ void* msdp_context_stream(const msdp_context* ctx) { return ctx ? (void*)ctx->st
 int msdp_batch_destroy(msdp_batch* b) {
   if (!b) return MSDP_OK;
   void* ptrs[] = {b->dprob, b->dblk, b->dorder, b->dd, b->d64, b->d32, b->erow, b->ecol,
-                  b->pcon,  b->eval, b->pval,   b->ptr, b->queue, b->scal};
+                  b->pcon,  b->eval, b->pval,   b->ptr, b->queue, b->scal, b->gsol, b->gseg};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete b;
@@ -529,6 +533,72 @@ int msdp_batch_get_all_stats(msdp_batch* b, msdp_stats* out) {
   int rc = gather(b, sc);
   if (rc) return rc;
   for (int p = 0; p < b->nprob; ++p) fill_stats(sc.data() + (size_t)p * SC_COUNT, out + p);
+  return MSDP_OK;
+}
+
+namespace {
+struct SolSeg {
+  const double* src;
+  int64_t dst, len;
+};
+// one block per segment: packed copy of the solution arrays
+__global__ void k_gather_solutions(const SolSeg* __restrict__ seg, double* __restrict__ out) {
+  const SolSeg s = seg[blockIdx.x];
+  for (int64_t i = threadIdx.x; i < s.len; i += blockDim.x) out[s.dst + i] = s.src[i];
+}
+
+// Segments in problem order: X of every block (column-major n x n), y, x, z.
+void solution_segments(msdp_batch* b, std::vector<SolSeg>* segs, int64_t* total) {
+  int64_t off = 0;
+  for (int p = 0; p < b->nprob; ++p) {
+    const ProbDesc& d = b->hprob[p];
+    for (int i = 0; i < d.nblocks; ++i) {
+      const int64_t n = b->hblk[d.blk0 + i].n;
+      segs->push_back({bmat64(b, p, i, M_X), off, n * n});
+      off += n * n;
+    }
+    if (d.m) segs->push_back({vec64(b, p, V_Y), off, d.m});
+    off += d.m;
+    if (d.ns) {
+      segs->push_back({svec64(b, p, S_X), off, d.ns});
+      segs->push_back({svec64(b, p, S_Z), off + d.ns, d.ns});
+    }
+    off += 2 * (int64_t)d.ns;
+  }
+  *total = off;
+}
+}  // namespace
+
+int64_t msdp_batch_solution_size(const msdp_batch* cb) {
+  if (!cb) return 0;
+  msdp_batch* b = const_cast<msdp_batch*>(cb);
+  std::vector<SolSeg> segs;
+  int64_t total = 0;
+  solution_segments(b, &segs, &total);
+  return total;
+}
+
+int msdp_batch_get_all_solutions(msdp_batch* b, double* out) {
+  if (!b || !out) return MSDP_ERR_INVALID_ARGUMENT;
+  msdp_context* ctx = b->ctx;
+  if (!b->gsol) {
+    std::vector<SolSeg> segs;
+    int64_t total = 0;
+    solution_segments(b, &segs, &total);
+    CK(cudaMalloc((void**)&b->gsol, sizeof(double) * (size_t)std::max<int64_t>(total, 1)));
+    CK(cudaMalloc(&b->gseg, sizeof(SolSeg) * std::max<size_t>(segs.size(), 1)));
+    CK(cudaMemcpy(b->gseg, segs.data(), sizeof(SolSeg) * segs.size(), cudaMemcpyHostToDevice));
+    b->nseg = (int64_t)segs.size();
+    b->sol_size = total;
+    b->bytes += sizeof(double) * total + sizeof(SolSeg) * segs.size();
+  }
+  if (b->nseg) {
+    k_gather_solutions<<<(unsigned)b->nseg, 128, 0, ctx->stream>>>((const SolSeg*)b->gseg, b->gsol);
+    CK(cudaGetLastError());
+    b->launches += 1;
+  }
+  CK(cudaMemcpyAsync(out, b->gsol, sizeof(double) * (size_t)b->sol_size, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   return MSDP_OK;
 }
 

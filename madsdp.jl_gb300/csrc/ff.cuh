@@ -32,7 +32,10 @@ struct ff {
   FF_HD constexpr ff(float h, float l) : hi(h), lo(l) {}
   // from a number: rounded to the nearest float-float (for double, hi is
   // the nearest float and lo the nearest float to the remainder)
-  FF_HD explicit ff(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+  // the nearest float, and the nearest float to the remainder; beyond the
+  // float range hi is infinite and lo is 0, so the value converts back to
+  // the same infinity
+  FF_HD explicit ff(double v) : hi((float)v), lo(hi - hi == 0.0f ? (float)(v - (double)hi) : 0.0f) {}
   FF_HD explicit ff(float v) : hi(v), lo(0.0f) {}
   FF_HD explicit ff(int v) : ff((double)v) {}
 };
@@ -118,7 +121,7 @@ FF_HD ff ff_sqrt(ff a) {
 // double <-> float-float (host-side conversions and tests)
 FF_HD ff ff_from_double(double v) {
   const float hi = (float)v;
-  return {hi, (float)(v - (double)hi)};
+  return {hi, hi - hi == 0.0f ? (float)(v - (double)hi) : 0.0f};
 }
 FF_HD double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 

@@ -26,7 +26,9 @@
 #include <vector>
 
 #include "../../include/madsdp_gpu.h"
+#include "chol.h"
 #include "la.cuh"
+#include "tcgemm.h"
 #include "tridiag.h"
 
 struct msdp_context;
@@ -254,20 +256,6 @@ __global__ void k_aff_lin(int ns, double a, double b, const double* x, const dou
 
 // svec of m symmetric n x n matrices (column-major upper triangle,
 // off-diagonal entries times sqrt 2): <B_j, B_k> = svec(B_j) . svec(B_k)
-__global__ void k_svec_pack(int n, int m, const double* __restrict__ Bm, double* __restrict__ Sv) {
-  const int64_t K = (int64_t)n * (n + 1) / 2, N = K * m;
-  const double r2 = 1.4142135623730951;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < N; idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t j = idx / K, t = idx % K;
-    int64_t q = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while (q * (q + 1) / 2 > t) --q;
-    while ((q + 1) * (q + 2) / 2 <= t) ++q;
-    const int64_t pr = t - q * (q + 1) / 2;
-    const double v = Bm[pr + q * n + j * (int64_t)n * n];
-    Sv[idx] = pr == q ? v : r2 * v;
-  }
-}
-
 // lambda_min of formed symmetric matrices Z (n <= 128), one warp per
 // matrix: Lanczos with full reorthogonalization and Sturm bisection of the
 // tridiagonal (the routine of the per-problem kernel), basis in global
@@ -315,6 +303,38 @@ __global__ void k_jtprod(int64_t nn, const int64_t* __restrict__ posptr, const i
   }
 }
 
+// ---- dense constraints stored as Aall (n^2 x m, column j = vec(A_j)) and
+// the m x ns C_lin: matrix-vector products that stream the matrix once.
+// out[i] = sum_j A[i + j lda] v[j]  (i < rows): thread per row, columns in order
+__global__ void k_gemv_n(int64_t rows, int cols, const double* __restrict__ A, int64_t lda,
+                         const double* __restrict__ v, double* __restrict__ out, int accumulate) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < cols; ++j) s = fma(A[i + j * lda], v[j], s);
+    out[i] = accumulate ? out[i] + s : s;
+  }
+}
+// out[j] (+)= sum_i A[i + j lda] v[i]  (j < cols): one block per column,
+// fixed reduction tree (deterministic)
+__global__ void k_gemv_t(int64_t rows, int cols, const double* __restrict__ A, int64_t lda,
+                         const double* __restrict__ v, double* __restrict__ out, int accumulate) {
+  __shared__ double red[kThreads / 32];
+  for (int j = blockIdx.x; j < cols; j += gridDim.x) {
+    const double* a = A + (int64_t)j * lda;
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < rows; i += blockDim.x) s = fma(a[i], v[i], s);
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+      out[j] = accumulate ? out[j] + t : t;
+    }
+    __syncthreads();
+  }
+}
+
 // H[j, k] += <A_j, L A_k R> for j >= k: sum over entry pairs
 // v_e v_f L[r_e, r_f] R[c_f, c_e] (the semantics of LowRankOpt's
 // schur_complement!, src/solver.jl:30-31,117-118).
@@ -355,6 +375,11 @@ struct Blk {
   int32_t *erow = nullptr, *ecol = nullptr, *pcon = nullptr;
   double *eval = nullptr, *pval = nullptr;
   double* Aall = nullptr;  // dense: n x (n m), column j*n.. of A_j
+  // dense constraints on the tensor cores (sliced once at creation):
+  // [A_1; ...; A_m] as rows (j, r) with K = n, in the FP64 (7) and, for the
+  // mixed precision, the mixed (3) slicing; HKM also vec(A_j) rows, K = n^2
+  tcg::Sliced stk[2], vec[2];
+  int2* kmap = nullptr;  // NT: symmetric-vector index -> (row, column), row >= column
 };
 
 }  // namespace
@@ -375,6 +400,16 @@ struct msdp_solver {
   double *x = nullptr, *z = nullptr, *dx = nullptr, *dz = nullptr, *Rdlin = nullptr, *zinv = nullptr;
   double *corrlin = nullptr, *vlin = nullptr, *ctv = nullptr, *wlin = nullptr;
   double *H = nullptr, *H0 = nullptr, *Tb = nullptr, *Bb = nullptr;
+  // tensor-core products: operand slices of the n x n products (tA, tB),
+  // the per-iteration operands of the dense assembly (tQ, tS), C_lin and
+  // C_lin diag(x/z) (tCl, tCw), the fixed-point workspace and error flag
+  tcg::Sliced tA, tB, tQ, tS, tCl[2], tCw;
+  void *tAm = nullptr, *tBm = nullptr, *tQm = nullptr, *tSm = nullptr, *tCwm = nullptr;
+  long long* tfix = nullptr;
+  int64_t tfix_len = 0;
+  int* terr = nullptr;
+  int64_t tc_products = 0;  // tensor-core products issued
+  chol::Work cw;            // blocked Cholesky (Schur matrix and blocks)
   double* work = nullptr;
   int lwork = 0;
   double *lq = nullptr, *lh = nullptr;  // Lanczos basis (n x (kLanczosMax + 1)) and projections
@@ -490,16 +525,71 @@ bool fetch(S* s) {
 void reset_slots(S* s) { s->nslot = 0; s->ninfo = 0; }
 int next_info(S* s) { return s->ninfo < kInfos ? s->ninfo++ : kInfos - 1; }
 
+// ---- tensor-core products (tcgemm.h)
+// Bind an operand's slices to rows x K (tensor maps re-encoded only when the
+// shape changes; the slicer writes every padded entry, so no clearing).
+bool tc_bind(S* s, tcg::Sliced* sl, void* mem, int64_t rows, int64_t K, int ns) {
+  if (sl->s && sl->rows == rows && sl->K == K && sl->ns == ns) return true;
+  const bool ok = tcg::sliced_init(sl, mem, rows, K, ns, s->st, false) == cudaSuccess;
+  note(s, ok, "tcg::sliced_init");
+  return ok;
+}
+void tc_slice(S* s, const tcg::Source& src, tcg::Sliced* sl) {
+  note(s, tcg::slice(src, sl, s->st) == cudaSuccess, "tcg::slice");
+  s->launches += 2;
+}
+void tc_product(S* s, const tcg::Sliced& A, const tcg::Sliced& B, tcg::Mode mode, double* C, int64_t ldc, double alpha,
+                double beta, bool lower) {
+  tcg::Out o;
+  o.C = C;
+  o.ldc = ldc;
+  o.alpha = alpha;
+  o.beta = beta;
+  o.lower = lower;
+  o.fix = s->tfix;
+  o.ldfix = A.rows;
+  o.err = s->terr;
+  if (tcg::needs_fix(A, B, mode, o) && A.rows * B.rows > s->tfix_len) {
+    note(s, false, "tensor-core product: fixed-point workspace too small");
+    return;
+  }
+  note(s, tcg::gemm(A, B, mode, o, s->st, &s->launches) == cudaSuccess, "tcg::gemm");
+  s->tc_products += 1;
+}
+// Row operand for op(M): element (r, k) of op(M) (rows x K), M column-major.
+tcg::Source op_rows(const double* Mp, int64_t ld, bool trans, int64_t rows, int64_t K) {
+  tcg::Source src;
+  src.p = Mp;
+  src.rows = rows;
+  src.K = K;
+  src.nr = rows;
+  src.bs = 0;
+  src.rs = trans ? ld : 1;
+  src.ks = trans ? 1 : ld;
+  return src;
+}
+tcg::Mode tc_mode(const S* s) { return s->comp.precision == MSDP_MIXED ? tcg::kMixed : tcg::kFp64; }
+
 // ---- dense linear algebra
+// C = alpha op(A) op(B) + beta C (FP64-accurate tensor-core product)
 void gemm(S* s, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k, double alpha, const double* A, int lda,
           const double* Bm, int ldb, double beta, double* C, int ldc) {
-  CB(s, cublasDgemm(s->cb, ta, tb, m, n, k, &alpha, A, lda, Bm, ldb, &beta, C, ldc));
+  if (!tc_bind(s, &s->tA, s->tAm, m, k, 7) || !tc_bind(s, &s->tB, s->tBm, n, k, 7)) return;
+  tc_slice(s, op_rows(A, lda, ta != CUBLAS_OP_N, m, k), &s->tA);
+  tc_slice(s, op_rows(Bm, ldb, tb == CUBLAS_OP_N, n, k), &s->tB);
+  tc_product(s, s->tA, s->tB, tcg::kFp64, C, ldc, alpha, beta, false);
+}
+// lower triangle of C = alpha op(A) op(A)' + beta C, op(A) n x k
+void syrk(S* s, bool trans, int n, int k, double alpha, const double* A, int lda, double beta, double* C, int ldc) {
+  if (!tc_bind(s, &s->tA, s->tAm, n, k, 7)) return;
+  tc_slice(s, op_rows(A, lda, trans, n, k), &s->tA);
+  tc_product(s, s->tA, s->tA, tcg::kFp64, C, ldc, alpha, beta, true);
 }
 
-// potrf of the lower triangle in place; returns the info index
-int potrf(S* s, int n, double* A, int lda) {
+// potrf of the lower triangle in place (chol.h); returns the info index
+int potrf(S* s, int n, double* A, int lda, tcg::Mode mode = tcg::kFp64) {
   const int k = next_info(s);
-  CS(s, cusolverDnDpotrf(s->cs, CUBLAS_FILL_MODE_LOWER, n, A, lda, s->work, s->lwork, s->dinfo + k));
+  note(s, chol::potrf(s->cw, n, A, lda, s->dinfo + k, mode, s->st, &s->launches) == cudaSuccess, "chol::potrf");
   return k;
 }
 
@@ -524,8 +614,9 @@ bool chol_ok(S* s, const CholCheck& c) { return s->hinfo[c.info] == 0 && s->hslo
 // ---- constraint operators of one block
 void jprod(S* s, Blk& b, const double* X, double* out, bool accumulate) {
   if (b.dense) {
-    const double one = 1.0, beta = accumulate ? 1.0 : 0.0;
-    CB(s, cublasDgemv(s->cb, CUBLAS_OP_T, b.n * b.n, s->m, &one, b.Aall, b.n * b.n, X, 1, &beta, out, 1));
+    const int64_t nn = (int64_t)b.n * b.n;
+    k_gemv_t<<<std::min(s->m, 152 * 16), kThreads, 0, s->st>>>(nn, s->m, b.Aall, nn, X, out, accumulate ? 1 : 0);
+    s->launches += 1;
   } else {
     LAUNCH(s, k_jprod, s->m, s->m, b.conptr, b.erow, b.ecol, b.eval, b.n, X, out, accumulate ? 1 : 0);
   }
@@ -534,8 +625,7 @@ void jprod(S* s, Blk& b, const double* X, double* out, bool accumulate) {
 void jtprod(S* s, Blk& b, const double* yv, double* out) {
   const int64_t nn = (int64_t)b.n * b.n;
   if (b.dense) {
-    const double one = 1.0, zero = 0.0;
-    CB(s, cublasDgemv(s->cb, CUBLAS_OP_N, b.n * b.n, s->m, &one, b.Aall, b.n * b.n, yv, 1, &zero, out, 1));
+    LAUNCH(s, k_gemv_n, nn, nn, s->m, b.Aall, nn, yv, out, 0);
   } else {
     LAUNCH(s, k_jtprod, nn, nn, b.posptr, b.pcon, b.pval, yv, out);
   }
@@ -562,10 +652,7 @@ bool update_residuals(S* s) {
   const int m = s->m, ns = s->ns;
   if (m) CU(s, cudaMemsetAsync(s->acc, 0, sizeof(double) * m, s->st));
   for (auto& b : s->B) jprod(s, b, b.X, s->acc, true);
-  if (ns && m) {
-    const double one = 1.0;
-    CB(s, cublasDgemv(s->cb, CUBLAS_OP_N, m, ns, &one, s->Clin, m, s->x, 1, &one, s->acc, 1));
-  }
+  if (ns && m) LAUNCH(s, k_gemv_n, m, m, ns, s->Clin, (int64_t)m, s->x, s->acc, 1);
   if (m) LAUNCH(s, k_lin, m, m, s->Rp, 1.0, s->b, -1.0, s->acc, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
   std::vector<int> rmax(s->nb);
   for (int i = 0; i < s->nb; ++i) {
@@ -576,9 +663,12 @@ bool update_residuals(S* s) {
     rmax[i] = reduce(s, RED_MAXABS, nn, b.Rd);
   }
   if (ns) {
-    const double one = 1.0, zero = 0.0;
-    if (m) CB(s, cublasDgemv(s->cb, CUBLAS_OP_T, m, ns, &one, s->Clin, m, s->y, 1, &zero, s->ctv, 1));
-    else CU(s, cudaMemsetAsync(s->ctv, 0, sizeof(double) * ns, s->st));
+    if (m) {
+      k_gemv_t<<<std::min(ns, 152 * 16), kThreads, 0, s->st>>>(m, ns, s->Clin, m, s->y, s->ctv, 0);
+      s->launches += 1;
+    } else {
+      CU(s, cudaMemsetAsync(s->ctv, 0, sizeof(double) * ns, s->st));
+    }
     LAUNCH(s, k_lin, ns, ns, s->Rdlin, 1.0, s->dlin, -1.0, s->z, -1.0, s->ctv, 0.0, nullptr, 0.0, nullptr);
   }
   if (!fetch(s)) return false;
@@ -664,8 +754,8 @@ bool prepare(S* s, bool* ok) {
     if (is_nt(s)) {
       // M = Ls' Lx ; N = M'M ; eig(N) = V diag(lam) V'
       gemm(s, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, 1.0, b.Ls, n, b.Lx, n, 0.0, b.T1, n);
-      const double one = 1.0, zero = 0.0;
-      CB(s, cublasDsyrk(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, n, n, &one, b.T1, n, &zero, b.T2, n));
+      const double one = 1.0;
+      syrk(s, true, n, n, 1.0, b.T1, n, 0.0, b.T2, n);
       const int ke = next_info(s);
       CS(s, cusolverDnDsyevd(s->cs, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, b.T2, n, b.lam, s->work,
                              s->lwork, s->dinfo + ke));
@@ -677,7 +767,7 @@ bool prepare(S* s, bool* ok) {
       LAUNCH(s, k_gi0, nn, n, b.T2, b.sc, b.Gi);
       CB(s, cublasDtrsm(s->cb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                         b.Lx, n, b.Gi, n));
-      CB(s, cublasDsyrk(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, n, &one, b.G, n, &zero, b.W, n));
+      syrk(s, false, n, n, 1.0, b.G, n, 0.0, b.W, n);
       LAUNCH(s, k_lower_to_full, nn, n, b.W);
     }
   }
@@ -695,38 +785,63 @@ bool prepare(S* s, bool* ok) {
   return !s->fail;
 }
 
-// H = sum_i <A_ij, L_i A_ik R_i> + C_lin diag(x/z) C_lin' (lower triangle)
-void schur_complement(S* s, double* H) {
+// H = sum_i <A_ij, L_i A_ik R_i> + C_lin diag(x/z) C_lin' (lower triangle).
+// Dense constraint blocks and the scalar block are products on the tensor
+// cores (tcgemm.h), in the FP64 slicing or, for the mixed precision, the
+// split-precision one; coordinate lists use the entry-pair kernel.
+void schur_complement(S* s, double* H, tcg::Mode mode) {
   const int m = s->m;
+  const int nsl = tcg::slices_of(mode), mi = mode == tcg::kMixed ? 1 : 0;
   CU(s, cudaMemsetAsync(H, 0, sizeof(double) * m * m, s->st));
-  const double one = 1.0, zero = 0.0;
   for (auto& b : s->B) {
     const int n = b.n;
     const double* L = is_nt(s) ? b.W : b.Si;
     const double* R = is_nt(s) ? b.W : b.X;
+    const int64_t mn = (int64_t)m * n;
     if (!b.dense) {
       LAUNCH(s, k_schur_pairs, (int64_t)m * (m + 1) / 2, m, b.conptr, b.erow, b.ecol, b.eval, n, L, R, H);
     } else if (is_nt(s)) {
-      // B_j = G' A_j G ; H += svec-free Gram matrix of the B_j
-      gemm(s, CUBLAS_OP_T, CUBLAS_OP_N, n, n * m, n, 1.0, b.G, n, b.Aall, n, 0.0, s->Tb, n);
-      CB(s, cublasDgemmStridedBatched(s->cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, s->Tb, n, (long long)n * n, b.G,
-                                      n, 0, &zero, s->Bb, n, (long long)n * n, m));
-      // H += svec(B)' svec(B): K = n(n+1)/2 instead of n^2 (T is free again)
-      const int K = n * (n + 1) / 2;
-      LAUNCH(s, k_svec_pack, (int64_t)K * m, n, m, s->Bb, s->Tb);
-      CB(s, cublasDsyrk(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, m, K, &one, s->Tb, K, &one, H, m));
+      // P = [A_1; ...; A_m] G (rows (j, r)), then B_j = (A_j G)' G, then
+      // H += svec(B)' svec(B) over K = n(n+1)/2 (off-diagonals x sqrt 2)
+      if (!tc_bind(s, &s->tB, s->tBm, n, n, nsl) || !tc_bind(s, &s->tQ, s->tQm, mn, n, nsl)) return;
+      tc_slice(s, op_rows(b.G, n, true, n, n), &s->tB);
+      tc_product(s, b.stk[mi], s->tB, mode, s->Tb, mn, 1.0, 0.0, false);
+      tcg::Source q;
+      q.p = s->Tb; q.rows = mn; q.K = n; q.nr = n; q.bs = n; q.rs = mn; q.ks = 1;
+      tc_slice(s, q, &s->tQ);
+      tc_product(s, s->tQ, s->tB, mode, s->Bb, mn, 1.0, 0.0, false);
+      const int64_t K = (int64_t)n * (n + 1) / 2;
+      if (!tc_bind(s, &s->tS, s->tSm, m, K, nsl)) return;
+      tcg::Source v;
+      v.p = s->Bb; v.rows = m; v.K = K; v.nr = 1; v.bs = n; v.rs = 1; v.ks = mn; v.kmap = b.kmap;
+      tc_slice(s, v, &s->tS);
+      tc_product(s, s->tS, s->tS, mode, H, m, 1.0, 1.0, true);
     } else {
-      // T_k = S^-1 A_k X ; H_jk += <A_j, T_k>
-      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n * m, n, 1.0, b.Si, n, b.Aall, n, 0.0, s->Tb, n);
-      CB(s, cublasDgemmStridedBatched(s->cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, s->Tb, n, (long long)n * n, b.X,
-                                      n, 0, &zero, s->Bb, n, (long long)n * n, m));
-      gemm(s, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n * n, 1.0, b.Aall, n * n, s->Bb, n * n, 1.0, H, m);
+      // P_k = A_k X (rows (k, r)), T_k = S^-1 P_k (side by side), H_jk += <A_j, T_k>
+      if (!tc_bind(s, &s->tB, s->tBm, n, n, nsl) || !tc_bind(s, &s->tA, s->tAm, n, n, nsl) ||
+          !tc_bind(s, &s->tQ, s->tQm, mn, n, nsl))
+        return;
+      tc_slice(s, op_rows(b.X, n, true, n, n), &s->tB);
+      tc_product(s, b.stk[mi], s->tB, mode, s->Tb, mn, 1.0, 0.0, false);
+      tc_slice(s, op_rows(b.Si, n, true, n, n), &s->tA);  // S^-1 is symmetric: rows read contiguously
+      tcg::Source q;
+      q.p = s->Tb; q.rows = mn; q.K = n; q.nr = n; q.bs = n; q.rs = mn; q.ks = 1;
+      tc_slice(s, q, &s->tQ);
+      tc_product(s, s->tA, s->tQ, mode, s->Bb, n, 1.0, 0.0, false);
+      const int64_t nn = (int64_t)n * n;
+      if (!tc_bind(s, &s->tS, s->tSm, m, nn, nsl)) return;
+      tcg::Source t;
+      t.p = s->Bb; t.rows = m; t.K = nn; t.nr = 1; t.bs = nn; t.rs = 0; t.ks = 1;
+      tc_slice(s, t, &s->tS);
+      tc_product(s, b.vec[mi], s->tS, mode, H, m, 1.0, 1.0, true);
     }
   }
   if (s->ns && m) {
     LAUNCH(s, k_mul, s->ns, s->ns, s->x, s->zinv, s->wlin);
     LAUNCH(s, k_scale_cols, (int64_t)m * s->ns, m, s->ns, s->Clin, s->wlin, s->Cw);
-    gemm(s, CUBLAS_OP_N, CUBLAS_OP_T, m, m, s->ns, 1.0, s->Cw, m, s->Clin, m, 1.0, H, m);
+    if (!tc_bind(s, &s->tCw, s->tCwm, m, s->ns, nsl)) return;
+    tc_slice(s, op_rows(s->Cw, m, false, m, s->ns), &s->tCw);
+    tc_product(s, s->tCl[mi], s->tCw, mode, H, m, 1.0, 1.0, true);
   }
 }
 
@@ -736,7 +851,7 @@ bool factorize_schur(S* s, bool* ok) {
   *ok = false;
   if (m == 0) { *ok = true; return true; }
   mark(s, PH_ASSEMBLY);
-  schur_complement(s, s->H0);
+  schur_complement(s, s->H0, tcg::kFp64);
   mark(s, PH_FACTOR);
   double reg = s->opt.regularize_schur;
   for (int t = 0; t < s->opt.max_schur_reg; ++t) {
@@ -755,7 +870,6 @@ bool factorize_schur(S* s, bool* ok) {
 // ---- directions (src/step.jl:63-124)
 void solve_directions(S* s, double mu, bool corrected) {
   const int m = s->m, ns = s->ns;
-  const double one = 1.0, zero = 0.0;
   // rhs
   if (m) CU(s, cudaMemcpyAsync(s->h, s->Rp, sizeof(double) * m, cudaMemcpyDeviceToDevice, s->st));
   for (auto& b : s->B) {
@@ -766,7 +880,7 @@ void solve_directions(S* s, double mu, bool corrected) {
   }
   if (ns && m) {
     LAUNCH(s, k_rhs_lin, ns, ns, mu, s->x, s->zinv, s->Rdlin, corrected ? s->corrlin : nullptr, s->vlin);
-    CB(s, cublasDgemv(s->cb, CUBLAS_OP_N, m, ns, &one, s->Clin, m, s->vlin, 1, &one, s->h, 1));
+    LAUNCH(s, k_gemv_n, m, m, ns, s->Clin, (int64_t)m, s->vlin, s->h, 1);
   }
   // dely = H^-1 h
   if (m) {
@@ -785,8 +899,12 @@ void solve_directions(S* s, double mu, bool corrected) {
     LAUNCH(s, k_sym, nn, b.n, b.dX);
   }
   if (ns) {
-    if (m) CB(s, cublasDgemv(s->cb, CUBLAS_OP_T, m, ns, &one, s->Clin, m, s->dy, 1, &zero, s->ctv, 1));
-    else CU(s, cudaMemsetAsync(s->ctv, 0, sizeof(double) * ns, s->st));
+    if (m) {
+      k_gemv_t<<<std::min(ns, 152 * 16), kThreads, 0, s->st>>>(m, ns, s->Clin, m, s->dy, s->ctv, 0);
+      s->launches += 1;
+    } else {
+      CU(s, cudaMemsetAsync(s->ctv, 0, sizeof(double) * ns, s->st));
+    }
     LAUNCH(s, k_dir_lin, ns, ns, mu, s->Rdlin, s->ctv, s->x, s->zinv, corrected ? s->corrlin : nullptr, s->dz, s->dx);
   }
 }
@@ -1101,9 +1219,12 @@ void set_dual_slacks(S* s) {
     LAUNCH(s, k_sym, nn, b.n, b.S);
   }
   if (s->ns) {
-    const double one = 1.0, zero = 0.0;
-    if (s->m) CB(s, cublasDgemv(s->cb, CUBLAS_OP_T, s->m, s->ns, &one, s->Clin, s->m, s->y, 1, &zero, s->ctv, 1));
-    else CU(s, cudaMemsetAsync(s->ctv, 0, sizeof(double) * s->ns, s->st));
+    if (s->m) {
+      k_gemv_t<<<std::min(s->ns, 152 * 16), kThreads, 0, s->st>>>(s->m, s->ns, s->Clin, s->m, s->y, s->ctv, 0);
+      s->launches += 1;
+    } else {
+      CU(s, cudaMemsetAsync(s->ctv, 0, sizeof(double) * s->ns, s->st));
+    }
     LAUNCH(s, k_lin, s->ns, s->ns, s->z, 1.0, s->dlin, -1.0, s->ctv, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
   }
 }
@@ -1183,6 +1304,93 @@ int initialize(S* s) {
   const double mu = tc / std::max(nu(s), 1);
   s->mu = s->comp.centering == MSDP_ADAPTIVE_MU ? s->comp.initial_ratio * mu : mu;
   return MSDP_OK;
+}
+
+// Tensor-core workspaces, and the slices of the constant constraint data
+// (dense blocks: [A_1; ...; A_m] rows, HKM also vec(A_j) rows; C_lin),
+// made once; nonzero on failure.
+int tc_setup(S* s, bool mixed) {
+  const int m = s->m, ns = s->ns;
+  int nmax = 1, nd = 0;
+  for (auto& b : s->B) {
+    nmax = std::max(nmax, b.n);
+    if (b.dense) nd = std::max(nd, b.n);
+  }
+  auto tcalloc = [&](int64_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMalloc(&p, (size_t)std::max<int64_t>(bytes, 256)) != cudaSuccess) return nullptr;
+    s->allocs.push_back(p);
+    s->bytes += bytes;
+    return p;
+  };
+  s->tAm = tcalloc(tcg::sliced_bytes(nmax, nmax, 7));
+  s->tBm = tcalloc(tcg::sliced_bytes(nmax, nmax, 7));
+  int64_t fixn = std::max<int64_t>((int64_t)nmax * nmax, (int64_t)m * m);
+  if (nd) {
+    const int64_t mn = (int64_t)m * nd;
+    s->tQm = tcalloc(tcg::sliced_bytes(mn, nd, 7));
+    s->tSm = tcalloc(tcg::sliced_bytes(m, is_nt(s) ? (int64_t)nd * (nd + 1) / 2 : (int64_t)nd * nd, 7));
+    if (!s->tQm || !s->tSm) return 1;
+    fixn = std::max(fixn, mn * nd);  // split-K operands of the assembly's first two products
+  }
+  if (ns && m) {
+    s->tCwm = tcalloc(tcg::sliced_bytes(m, ns, 7));
+    if (!s->tCwm) return 1;
+  }
+  s->tfix = (long long*)tcalloc(8 * fixn);
+  s->tfix_len = fixn;
+  s->terr = (int*)tcalloc(sizeof(int));
+  void* cwm = tcalloc(chol::work_bytes(std::max(nmax, m)));
+  if (!s->tAm || !s->tBm || !s->tfix || !s->terr || !cwm) return 1;
+  CU(s, chol::init(&s->cw, cwm, std::max(nmax, m), s->terr, s->st));
+  // the constraint data went up by synchronous copies from pageable memory
+  CU(s, cudaDeviceSynchronize());
+  CU(s, cudaMemsetAsync(s->terr, 0, sizeof(int), s->st));
+  const int nmodes = mixed ? 2 : 1;
+  for (auto& b : s->B) {
+    if (!b.dense) continue;
+    const int n = b.n;
+    const int64_t mn = (int64_t)m * n, nn = (int64_t)n * n;
+    for (int mi = 0; mi < nmodes; ++mi) {
+      const int nsl = mi ? 3 : 7;
+      void* mem = tcalloc(tcg::sliced_bytes(mn, n, nsl));
+      if (!mem) return 1;
+      CU(s, tcg::sliced_init(&b.stk[mi], mem, mn, n, nsl, s->st));
+      // row (j, r), column k: A_j(r, k) = A_j(k, r) = Aall[j n^2 + k + r n]
+      tcg::Source a;
+      a.p = b.Aall; a.rows = mn; a.K = n; a.nr = n; a.bs = nn; a.rs = n; a.ks = 1;
+      tc_slice(s, a, &b.stk[mi]);
+      if (!is_nt(s)) {
+        void* vm = tcalloc(tcg::sliced_bytes(m, nn, nsl));
+        if (!vm) return 1;
+        CU(s, tcg::sliced_init(&b.vec[mi], vm, m, nn, nsl, s->st));
+        tcg::Source v;
+        v.p = b.Aall; v.rows = m; v.K = nn; v.nr = 1; v.bs = nn; v.rs = 0; v.ks = 1;
+        tc_slice(s, v, &b.vec[mi]);
+      }
+    }
+    if (is_nt(s)) {
+      // symmetric-vector order: column c, then rows r >= c
+      std::vector<int2> km;
+      km.reserve((size_t)(nn + n) / 2);
+      for (int c = 0; c < n; ++c)
+        for (int r = c; r < n; ++r) km.push_back(make_int2(r, c));
+      b.kmap = (int2*)tcalloc((int64_t)sizeof(int2) * km.size());
+      if (!b.kmap) return 1;
+      CU(s, cudaMemcpy(b.kmap, km.data(), sizeof(int2) * km.size(), cudaMemcpyHostToDevice));
+    }
+  }
+  if (ns && m) {
+    for (int mi = 0; mi < nmodes; ++mi) {
+      const int nsl = mi ? 3 : 7;
+      void* mem = tcalloc(tcg::sliced_bytes(m, ns, nsl));
+      if (!mem) return 1;
+      CU(s, tcg::sliced_init(&s->tCl[mi], mem, m, ns, nsl, s->st));
+      tc_slice(s, op_rows(s->Clin, m, false, m, ns), &s->tCl[mi]);
+    }
+  }
+  CU(s, cudaStreamSynchronize(s->st));
+  return s->fail ? 1 : 0;
 }
 
 void release(S* s) {
@@ -1387,6 +1595,7 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   if (ns) CU(s, cudaMemcpy(s->dlin, d->d_lin, 8 * ns, cudaMemcpyHostToDevice));
   if (ns && m) CU(s, cudaMemcpy(s->Clin, d->C_lin, 8 * (int64_t)m * ns, cudaMemcpyHostToDevice));
   if (s->fail) return bail(s->fail);
+  if (tc_setup(s, c.precision == MSDP_MIXED)) return bail(s->fail ? s->fail : MSDP_ERR_OUT_OF_MEMORY);
   *out = s;
   return MSDP_OK;
 }

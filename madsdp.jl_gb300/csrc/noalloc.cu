@@ -120,14 +120,27 @@ extern "C" int msdp_solve_static(const msdp_problem_desc* prob, const msdp_compo
   if (c.initial_point == MSDP_INITIAL_POINT) return MSDP_ERR_UNSUPPORTED;
   cudaStream_t st = (cudaStream_t)stream_ptr;
 
-  // ---- layout inside the scratch (byte offsets)
+  // ---- sizes: every factor of the layout below is bounded first, so the
+  // int64 offsets cannot overflow for any int32 side or count
+  if (8 * (int64_t)m * m > kScratchBytes || 8 * (int64_t)m * ns > kScratchBytes) return MSDP_ERR_TOO_LARGE;
   int64_t total_nnz = 0, nn_sum = 0;
   for (int i = 0; i < nb; ++i) {
     const int64_t n = prob->sides[i];
     if (n <= 0 || prob->A_nnz[i] < 0) return MSDP_ERR_INVALID_ARGUMENT;
+    if (8 * n * n > kScratchBytes || prob->A_nnz[i] > kScratchBytes / 52) return MSDP_ERR_TOO_LARGE;
     total_nnz += prob->A_nnz[i];
     nn_sum += n * n;
   }
+  if (total_nnz > kScratchBytes / 52 || 8 * nn_sum > kScratchBytes) return MSDP_ERR_TOO_LARGE;
+  // the coordinate lists must be in range: checked before anything is
+  // enqueued, so a rejected call leaves the shared array as it was
+  for (int i = 0; i < nb; ++i)
+    for (int64_t q = 0; q < prob->A_nnz[i]; ++q)
+      if (prob->A_con[i][q] < 0 || prob->A_con[i][q] >= m || prob->A_row[i][q] < 0 ||
+          prob->A_row[i][q] >= prob->sides[i] || prob->A_col[i][q] < 0 || prob->A_col[i][q] >= prob->sides[i])
+        return MSDP_ERR_INVALID_ARGUMENT;
+
+  // ---- layout inside the scratch (byte offsets)
   ProbDesc pd;
   BlockDesc bds[MSDP_STATIC_MAX_BLOCKS];
   std::memset(&pd, 0, sizeof(pd));
@@ -210,12 +223,6 @@ extern "C" int msdp_solve_static(const msdp_problem_desc* prob, const msdp_compo
     up(o_rval + sizeof(double) * bd.ent, prob->A_val[i], sizeof(double) * bd.nnz);
   }
   if (e != cudaSuccess) return MSDP_ERR_CUDA;
-  // the coordinate lists must be in range (checked on the host, no copy kept)
-  for (int i = 0; i < nb; ++i)
-    for (int64_t q = 0; q < prob->A_nnz[i]; ++q)
-      if (prob->A_con[i][q] < 0 || prob->A_con[i][q] >= m || prob->A_row[i][q] < 0 ||
-          prob->A_row[i][q] >= prob->sides[i] || prob->A_col[i][q] < 0 || prob->A_col[i][q] >= prob->sides[i])
-        return MSDP_ERR_INVALID_ARGUMENT;
 
   BatchDev B;
   std::memset(&B, 0, sizeof(B));

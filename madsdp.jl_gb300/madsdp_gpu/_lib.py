@@ -81,6 +81,8 @@ SIGNATURES = [
     ("msdp_batch_get_stats", i32, [C.c_void_p, i32, P(Stats)]),
     ("msdp_batch_get_all_stats", i32, [C.c_void_p, P(Stats)]),
     ("msdp_batch_get_solution", i32, [C.c_void_p, i32, P(P(f64)), P(f64), P(f64), P(f64)]),
+    ("msdp_batch_solution_size", i64, [C.c_void_p]),
+    ("msdp_batch_get_all_solutions", i32, [C.c_void_p, P(f64)]),
     ("msdp_batch_get_trajectory", i32, [C.c_void_p, i32, P(IterRecord), i32, P(i32)]),
     ("msdp_batch_update_residuals", i32, [C.c_void_p]),
     ("msdp_batch_prepare", i32, [C.c_void_p, P(i32)]),
@@ -115,6 +117,9 @@ SIGNATURES = [
     ("msdp_solver_profile_field_name", C.c_char_p, [i32]),
     ("msdp_solver_launch_count", i64, [C.c_void_p]),
     ("msdp_solver_last_error", C.c_char_p, [C.c_void_p]),
+    ("msdp_dense_cholesky", i32, [i32, i32, C.c_void_p, i64, P(i32), C.c_void_p]),
+    ("msdp_tc_gemm", i32, [i32, i32, i32, i64, i64, i64, f64, C.c_void_p, i64, C.c_void_p, i64, f64, C.c_void_p, i64,
+                           i32, C.c_void_p]),
 ]
 
 _lib = None

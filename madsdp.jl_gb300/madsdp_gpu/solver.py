@@ -397,6 +397,26 @@ class Batch:
         self.ctx.check(rc, "msdp_batch_get_solution")
         return [np.ascontiguousarray(a) for a in X], y, x, z
 
+    def all_solutions(self) -> list:
+        """(X blocks, y, x, z) of every problem from one packed download;
+        the arrays are views of one host buffer."""
+        total = int(self.lib.msdp_batch_solution_size(self.h))
+        buf = np.empty(max(total, 1))
+        rc = self.lib.msdp_batch_get_all_solutions(self.h, _ptr(buf))
+        self.ctx.check(rc, "msdp_batch_get_all_solutions")
+        out, off = [], 0
+        for m in self.models:
+            X = []
+            for n in m.sides:
+                X.append(buf[off:off + n * n].reshape(n, n, order="F"))
+                off += n * n
+            y = buf[off:off + m.m]
+            off += m.m
+            x, z = buf[off:off + m.ns], buf[off + m.ns:off + 2 * m.ns]
+            off += 2 * m.ns
+            out.append((X, y, x, z))
+        return out
+
     def trajectory(self, p: int) -> List[dict]:
         cap = self.opt.max_iter + 2
         arr = (_lib.IterRecord * cap)()

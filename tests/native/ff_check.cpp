@@ -117,3 +117,13 @@ int ff_constructors(int64_t n, const double* a, const double* b, const double* c
 }
 
 }  // extern "C"
+
+extern "C" {
+// double -> float-float -> double through the constructor and ff_from_double
+void ff_roundtrip(int64_t n, const double* in, double* out_ctor, double* out_from) {
+  for (int64_t i = 0; i < n; ++i) {
+    out_ctor[i] = ff_to_double(ff(in[i]));
+    out_from[i] = ff_to_double(ff_from_double(in[i]));
+  }
+}
+}  // extern "C"

@@ -129,3 +129,30 @@ def test_constructors_and_fma(lib):
     rng = np.random.default_rng(9)
     a, b, c = values(rng, 2000), values(rng, 2000), values(rng, 2000)
     assert lib.ff_constructors(a.size, a.ctypes.data_as(D), b.ctypes.data_as(D), c.ctypes.data_as(D)) == 0
+
+
+def test_conversion_beyond_float_range(lib):
+    """Values beyond the float range become the infinity of their sign (not
+    NaN); finite values round-trip to within float-float precision."""
+    lib.ff_roundtrip.argtypes = [C.c_int64, D, D, D]
+    v = np.array([1e300, -1e300, np.inf, -np.inf, 3.5e38, 1.0 / 3.0, -2.0 ** -100, 0.0])
+    a, b = np.zeros_like(v), np.zeros_like(v)
+    lib.ff_roundtrip(v.size, v.ctypes.data_as(D), a.ctypes.data_as(D), b.ctypes.data_as(D))
+    for out in (a, b):
+        assert np.array_equal(out[:5], [np.inf, -np.inf, np.inf, -np.inf, np.inf])
+        assert np.all(np.abs(out[5:] - v[5:]) <= 2.0 ** -47 * np.abs(v[5:]))
+
+
+def test_cta_cholesky_instantiates_with_float_float(tmp_path):
+    """The CTA Cholesky of la.cuh compiles for sm_103a with T = ff (compile
+    only; nothing is launched)."""
+    import shutil
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc) and shutil.which(nvcc) is None:
+        pytest.skip("nvcc not available")
+    r = subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                        "--expt-relaxed-constexpr", "-Xptxas", "-v", "-c",
+                        os.path.join(HERE, "native", "ff_potrf_compile.cu"), "-o", str(tmp_path / "p.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "ff_potrf_probe" in r.stderr and "registers" in r.stderr

@@ -5,7 +5,12 @@ same result as the allocating entry point (msdp_batch_create +
 msdp_batch_solve) within the tolerance of the other parity tests, on two
 calls in a row (the static scratch array is reused and re-zeroed).
 
+It is also checked directly against the oracle, on entries that arrive in
+any order, for the property it exists for (a repeat call allocates no device
+memory) and for its argument checks.
+
 Collected last on purpose; it also passes alone in a fresh process."""
+import copy
 import ctypes as C
 
 import numpy as np
@@ -16,6 +21,13 @@ from madsdp_gpu import _lib, generators as g
 from madsdp_gpu.solver import _Marshalled, _components, _options, _ptr
 
 pytestmark = pytest.mark.gpu
+
+
+def static_status(model):
+    lib = _lib.load()
+    mm = _Marshalled(model)
+    st = _lib.Stats()
+    return lib.msdp_solve_static(C.byref(mm.desc), None, None, None, None, None, None, None, C.byref(st))
 
 
 def static_solve(model):
@@ -60,3 +72,55 @@ def test_static_rejects_oversize(gpu_ctx):
     st = _lib.Stats()
     rc = lib.msdp_solve_static(C.byref(mm.desc), None, None, None, None, None, None, None, C.byref(st))
     assert rc == -6
+
+
+def test_static_matches_oracle(gpu_ctx):
+    from oracle import madsdp_oracle as o
+    model = g.sos_hankel(11, seed=3)
+    ref = o.Solver(model).solve()
+    st, X, y, x, z = static_solve(model)
+    assert st.status == M.Status.SOLVE_SUCCEEDED
+    scale = max(1.0, abs(ref.primal_objective()) + abs(ref.dual_objective()))
+    assert abs(st.iter - ref.iter) <= 1
+    assert abs(st.pobj - ref.primal_objective()) <= 1e-7 * scale
+    assert abs(st.dobj - ref.dual_objective()) <= 1e-7 * scale
+
+
+def test_static_entry_order_does_not_matter(gpu_ctx):
+    """The entries of a constraint list may arrive in any order: the device
+    staging orders them, so the result equals the batch path's."""
+    model = g.dense_random([5, 3], 2, 8, seed=4)
+    ref = M.Batch([model])
+    ref.solve()
+    rs = ref.all_stats()[0]
+    shuffled = copy.deepcopy(model)
+    rng = np.random.default_rng(0)
+    for blk in shuffled.A:
+        perm = rng.permutation(blk.nnz)
+        blk.con, blk.row, blk.col = blk.con[perm].copy(), blk.row[perm].copy(), blk.col[perm].copy()
+        blk.val = blk.val[perm].copy()
+    st, X, y, x, z = static_solve(shuffled)
+    scale = max(1.0, abs(rs["pobj"]) + abs(rs["dobj"]))
+    assert st.status == M.Status.SOLVE_SUCCEEDED
+    assert abs(st.pobj - rs["pobj"]) <= 1e-7 * scale
+    assert abs(st.dobj - rs["dobj"]) <= 1e-7 * scale
+
+
+def test_static_repeat_call_allocates_nothing(gpu_ctx):
+    import torch
+    model = g.maxcut(20, 0.3, seed=8)
+    static_solve(model)            # first call: per-device set-up
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    static_solve(model)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+
+
+def test_static_rejects_out_of_range_entries(gpu_ctx):
+    model = copy.deepcopy(g.maxcut(10, 0.3, seed=2))
+    blk = model.A[0]
+    blk.con = blk.con.copy()
+    blk.con[0] = model.m            # constraint index past m
+    assert static_status(model) == -1
