@@ -226,6 +226,19 @@ def instance_flops_per_iteration(model) -> float:
     return f
 
 
+def assembly_flops_per_iteration(model) -> float:
+    """FP64-equivalent flops of the tensor-core Schur assembly of dense
+    blocks (NT): P = [A_1; ...; A_m] G and B_j = (A_j G)' G (2 m n^3 each),
+    then H += svec(B)' svec(B) over the lower triangle (m^2 n(n+1)/2), plus
+    the scalar block C_lin diag(x/z) C_lin' (m^2 ns)."""
+    m = model.m
+    f = float(m) * m * model.ns
+    for n, A in zip(model.sides, model.A):
+        if A.nnz >= m * n * n // 2:
+            f += 4.0 * m * n ** 3 + float(m) * m * n * (n + 1) / 2.0
+    return f
+
+
 def _oracle_iterations(spec, seed, q):
     sys.path[:0] = [ROOT, PKG]
     from oracle import madsdp_oracle as o
@@ -365,10 +378,7 @@ def run_instance(args):
     stream = torch.cuda.ExternalStream(ctx.stream_handle, device=torch.device("cuda", 0))
     # the engine MadSDPSolver(model) picks: one thread block (a one-problem
     # batch) for small problems, the whole-GPU solver for large ones
-    if args.precision == "mixed":
-        engine = "batch"
-    else:
-        engine = "instance" if (args.precision == "fp64_tensor" or M.solver._use_instance_engine(model)) else "batch"
+    engine = "instance" if (args.precision == "fp64_tensor" or M.solver._use_instance_engine(model)) else "batch"
     if engine == "instance":
         solver = M.InstanceSolver(model, context=ctx, precision=args.precision)
         run = solver.solve
@@ -411,6 +421,21 @@ def run_instance(args):
     t_solve = statistics.mean(ms) / 1000.0
     flops = instance_flops_per_iteration(model) * st["iter"]
     fp64_peak, _ = measured_fp_rates()  # GFLOP/s
+    # the tensor-core Schur assembly against the bf16 peak: slice products
+    # (28 for FP64-accurate, 6 for split precision) x FP64-equivalent flops
+    tc_assembly = None
+    if engine == "instance" and phases and phases.get("schur_assembly"):
+        af = assembly_flops_per_iteration(model) * st["iter"]
+        if af > 0:
+            hbm, bf16, peak_kind = measured_peaks()
+            n32, n64 = st.get("iter_fp32", 0), st.get("iter_fp64", 0)
+            pairs = (28.0 * n64 + 6.0 * n32) / max(1, n32 + n64)
+            tensor_tflops = af * pairs / phases["schur_assembly"] / 1e12
+            tc_assembly = {"fp64_equiv_tflops": af / phases["schur_assembly"] / 1e12,
+                           "tensor_tflops": tensor_tflops, "bf16_peak_tflops": bf16,
+                           "frac_of_bf16_peak": tensor_tflops / bf16, "peak_kind": f"{peak_kind} bf16 dense (burst)",
+                           "slice_products_per_flop": pairs,
+                           "note": "assembly phase device time (includes the slicing passes and the scalar block)"}
     cpu_block = port_block(*port) if port is not None else None
     if cpu is not None:
         per_it, nit, init = cpu
@@ -430,8 +455,13 @@ def run_instance(args):
         "data": "synthetic",
         "config": {"workload": args.workload, "precision": args.precision, **{k: v for k, v in spec.items() if k != "kind"}, "seed": args.seed,
                    "m": model.m, "components": "PrimalDual(NT, EigenStep, Mehrotra) + DenseCholesky, ScaledIdentity",
-                   "engine": ("whole-GPU instance solver (cuBLAS/cuSOLVER dense algebra + own assembly/residual kernels)"
-                              if engine == "instance" else "one thread block (persistent batch kernel, one problem)"),
+                   "engine": ("whole-GPU instance solver: tensor-core split-bf16 products and Schur assembly (tcgen05), "
+                              "blocked Cholesky with tensor-core updates and own triangular solves, own assembly/"
+                              "residual kernels; cuSOLVER eigensolver and S^-1, cuBLAS triangular solves of the "
+                              "step lengths" if engine == "instance"
+                              else "one thread block (persistent batch kernel, one problem)"),
+                   "iterations_fp32_schur": st.get("iter_fp32"), "iterations_fp64_schur": st.get("iter_fp64"),
+                   "tensor_core_assembly": tc_assembly,
                    "status": str(st["status"]), "iterations": st["iter"], "pobj": st["pobj"], "gap": st["gap"],
                    "inf_pr": st["inf_pr"], "inf_du": st["inf_du"], "phase_seconds_last_solve": phases,
                    "l2": f"{device_bytes / 2**20:.0f} MiB resident"},

@@ -321,6 +321,56 @@ const char* msdp_solver_profile_field_name(int32_t index);
 int64_t msdp_solver_launch_count(const msdp_solver* solver);
 const char* msdp_solver_last_error(const msdp_solver* solver);
 
+/* ---- component-granular calls on a whole-GPU solver ---------------------------
+ * For running one GPU component beside the reference's CPU components, and
+ * for identity tests.  The iterate is the one set last (or the solver's).
+ *   msdp_solver_set_iterate       X, S, y, x, z of the host driver; updates
+ *                                 the residuals (src/step.jl:12-47)
+ *   msdp_solver_prepare           _prepare! (src/primal_dual.jl:29-37):
+ *                                 chol(S) with the flush and S^-1
+ *                                 (src/blocks.jl:94-130), the NT scaling
+ *                                 W, G, D (src/directions.jl:45-75) and
+ *                                 chol(X) for EigenStep; *ok as the reference
+ *   msdp_solver_schur_assemble    LowRankOpt.schur_complement!(model, L, R, H)
+ *                                 (called at src/solver.jl:304) with the
+ *                                 prepared scaling, plus C_lin diag(x/z) C_lin';
+ *                                 the lower triangle of H (m x m column-major)
+ *                                 is written; MSDP_MIXED (NT, mixed-precision
+ *                                 solvers) gives the split-precision assembly
+ *   msdp_solver_get_block_matrix  the prepared W, G, S^-1, Ls, Lx (n x n) or D (n)
+ *   msdp_solver_step_eig          lambda_min(L^-1 D L^-T) of EigenStep
+ *                                 (src/step.jl:150-183) for a lower-triangular
+ *                                 L and symmetric D of the block's size */
+enum msdp_solver_matrix { MSDP_SMAT_W = 0, MSDP_SMAT_G = 1, MSDP_SMAT_SINV = 2, MSDP_SMAT_LS = 3, MSDP_SMAT_LX = 4,
+                          MSDP_SMAT_D = 5 };
+int msdp_solver_set_iterate(msdp_solver* solver, const double* const* X, const double* const* S, const double* y,
+                            const double* x, const double* z);
+int msdp_solver_prepare(msdp_solver* solver, int32_t* ok);
+int msdp_solver_schur_assemble(msdp_solver* solver, int32_t precision, double* H);
+int msdp_solver_get_block_matrix(msdp_solver* solver, int32_t block, int32_t which, double* out);
+int msdp_solver_step_eig(msdp_solver* solver, int32_t block, const double* L, const double* D, double* lambda_min);
+
+/* ---- a Schur-solver component (src/components.jl:253-266) ----------------------
+ *   msdp_schur_create     schur_workspace(DenseCholesky(), Float64, m)
+ *                         (src/schur_solvers.jl:10-14) on the device
+ *   msdp_schur_factorize  factorize!(ws) (src/schur_solvers.jl:15-19) of the
+ *                         host-assembled H (m x m column-major, lower
+ *                         triangle read, Hermitian(H, :L)); *success =
+ *                         issuccess
+ *   msdp_schur_solve      schur_solve!(ws, rhs) (src/schur_solvers.jl:21):
+ *                         rhs (m, host) is overwritten by the solution
+ * MSDP_MIXED: FP32-class factor, each solve refined against H in FP64 until
+ * the residual stops shrinking; a residual above 1e-11 |rhs| then refactors H
+ * in FP64 for the remaining solves of this factorization, and a breakdown of
+ * the FP32-class factorization falls back to FP64 at once
+ * (msdp_schur_fp64_active reports either). */
+typedef struct msdp_schur msdp_schur;
+int msdp_schur_create(msdp_context* ctx, int32_t m, int32_t precision, msdp_schur** ws);
+int msdp_schur_destroy(msdp_schur* ws);
+int msdp_schur_factorize(msdp_schur* ws, const double* H, int32_t* success);
+int msdp_schur_solve(msdp_schur* ws, double* rhs);
+int msdp_schur_fp64_active(const msdp_schur* ws);
+
 /* ---- split-precision products on the tensor cores ---------------------------
  * C = alpha op(A) op(B) + beta C for column-major float64 device arrays
  * (op = transpose when trans != 0), computed from bf16 slices of A and B on

@@ -110,13 +110,109 @@ __global__ void k_put_diag(int n, double* __restrict__ A, int64_t lda, const dou
   }
 }
 
+// Inverse of each factored diagonal block (one thread block of NB warps per
+// block; warp c forms column c row by row with a warp sum).
+__global__ void __launch_bounds__(NB * 32) k_diag_inverse(int n, const double* __restrict__ diag,
+                                                          double* __restrict__ dinv, const int* __restrict__ info) {
+  if (*info != 0) return;
+  __shared__ double Ls[NB][NB + 1], inv[NB][NB + 1];
+  const int64_t k0 = (int64_t)blockIdx.x * NB;
+  const int kb = (int)min((int64_t)NB, (int64_t)n - k0);
+  const int t = threadIdx.x, lane = t & 31, c = t >> 5;
+  {
+    const int r = t % NB, cc = t / NB;
+    Ls[r][cc] = diag[k0 * NB + t];  // column-major NB x NB block
+    inv[r][cc] = 0.0;
+  }
+  __syncthreads();
+  for (int r = 0; r < kb; ++r) {
+    double term = (lane >= c && lane < r) ? Ls[r][lane] * inv[lane][c] : 0.0;
+    for (int o = 16; o; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+    if (lane == 0 && c <= r) inv[r][c] = ((r == c ? 1.0 : 0.0) - term) / Ls[r][r];
+    __syncthreads();
+  }
+  {
+    const int r = t % NB, cc = t / NB;
+    dinv[k0 * NB + t] = (r < kb && cc < kb) ? inv[r][cc] : 0.0;
+  }
+}
+
+// x <- L^-T L^-1 x with the factor in L (lower) and the inverses of its
+// diagonal blocks; one thread block, block row by block row.  The sums over
+// the solved part read NB consecutive entries per column (coalesced), four
+// independent accumulators per thread.
+__global__ void __launch_bounds__(1024) k_chol_solve(int n, const double* __restrict__ L, int64_t ld,
+                                                     const double* __restrict__ dinv, double* x,
+                                                     const int* __restrict__ info) {
+  if (*info != 0) return;
+  __shared__ double red[32][33];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int nbk = (n + NB - 1) / NB;
+  // forward: L y = x
+  for (int b = 0; b < nbk; ++b) {
+    const int r0 = b * NB, rows = min(NB, n - r0);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (lane < rows) {
+      const double* Lr = L + r0 + lane;
+      int c = w;
+      for (; c + 96 < r0; c += 128) {
+        a0 = fma(Lr[(int64_t)c * ld], x[c], a0);
+        a1 = fma(Lr[(int64_t)(c + 32) * ld], x[c + 32], a1);
+        a2 = fma(Lr[(int64_t)(c + 64) * ld], x[c + 64], a2);
+        a3 = fma(Lr[(int64_t)(c + 96) * ld], x[c + 96], a3);
+      }
+      for (; c < r0; c += 32) a0 = fma(Lr[(int64_t)c * ld], x[c], a0);
+    }
+    red[w][lane] = (a0 + a1) + (a2 + a3);
+    __syncthreads();
+    if (w == 0) {
+      double sum = 0.0;
+      for (int g = 0; g < 32; ++g) sum += red[g][lane];
+      const double v = lane < rows ? x[r0 + lane] - sum : 0.0;
+      const double* Di = dinv + (int64_t)b * NB * NB;
+      double y = 0.0;
+      for (int c = 0; c < NB; ++c) y = fma(Di[lane + c * NB], __shfl_sync(0xffffffffu, v, c), y);
+      if (lane < rows) x[r0 + lane] = y;
+    }
+    __syncthreads();
+  }
+  // backward: L' z = y
+  for (int b = nbk - 1; b >= 0; --b) {
+    const int r0 = b * NB, rows = min(NB, n - r0);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (w < rows) {
+      const double* Lc = L + (int64_t)(r0 + w) * ld;
+      int j = r0 + NB + lane;
+      for (; j + 96 < n; j += 128) {
+        a0 = fma(Lc[j], x[j], a0);
+        a1 = fma(Lc[j + 32], x[j + 32], a1);
+        a2 = fma(Lc[j + 64], x[j + 64], a2);
+        a3 = fma(Lc[j + 96], x[j + 96], a3);
+      }
+      for (; j < n; j += 32) a0 = fma(Lc[j], x[j], a0);
+    }
+    double a = (a0 + a1) + (a2 + a3);
+    for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) red[0][w] = a;
+    __syncthreads();
+    if (w == 0) {
+      const double v = lane < rows ? x[r0 + lane] - red[0][lane] : 0.0;
+      const double* Di = dinv + (int64_t)b * NB * NB;
+      double y = 0.0;
+      for (int c = 0; c < NB; ++c) y = fma(Di[c + lane * NB], __shfl_sync(0xffffffffu, v, c), y);
+      if (lane < rows) x[r0 + lane] = y;
+    }
+    __syncthreads();
+  }
+}
+
 int64_t panel_bytes(int64_t nmax) { return tcg::sliced_bytes(nmax, NB, 7); }
 
 }  // namespace
 
 int64_t work_bytes(int64_t nmax) {
   nmax = std::max<int64_t>(nmax, 1);
-  return panel_bytes(nmax) + (nmax + NB) * NB * 8;
+  return panel_bytes(nmax) + 2 * (nmax + NB) * NB * 8;
 }
 
 cudaError_t init(Work* w, void* mem, int64_t nmax, int* err, cudaStream_t st) {
@@ -124,7 +220,17 @@ cudaError_t init(Work* w, void* mem, int64_t nmax, int* err, cudaStream_t st) {
   w->nmax = std::max<int64_t>(nmax, 1);
   w->err = err;
   w->diag = (double*)((char*)mem + panel_bytes(w->nmax));
+  w->dinv = w->diag + (w->nmax + NB) * NB;
   return tcg::sliced_init(&w->panel, mem, w->nmax, NB, 7, st);
+}
+
+cudaError_t solve(const Work& w, int n, const double* L, int64_t ld, double* x, const int* info, cudaStream_t st,
+                  int64_t* launches) {
+  if (n <= 0) return cudaSuccess;
+  if (n > w.nmax) return cudaErrorInvalidValue;
+  k_chol_solve<<<1, 1024, 0, st>>>(n, L, ld, w.dinv, x, info);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
 }
 
 cudaError_t potrf(Work& w, int n, double* A, int64_t lda, int* info, tcg::Mode mode, cudaStream_t st,
@@ -165,7 +271,8 @@ cudaError_t potrf(Work& w, int n, double* A, int64_t lda, int* info, tcg::Mode m
   if (n > 0) {
     const int64_t total = (int64_t)((n + NB - 1) / NB) * NB * NB;
     k_put_diag<<<(unsigned)std::min<int64_t>((total + 255) / 256, 1024), 256, 0, st>>>(n, A, lda, w.diag, info);
-    if (launches) *launches += 1;
+    k_diag_inverse<<<(unsigned)((n + NB - 1) / NB), NB * 32, 0, st>>>(n, w.diag, w.dinv, info);
+    if (launches) *launches += 2;
     e = cudaGetLastError();
   }
   return e;

@@ -24,6 +24,7 @@ struct Work {
   tcg::Sliced panel;     // slices of the panel below the diagonal block (K = 32)
   void* mem = nullptr;
   double* diag = nullptr;  // factored diagonal blocks (NB x NB per block column)
+  double* dinv = nullptr;  // their inverses (the triangular solves)
   int64_t nmax = 0;
   int* err = nullptr;    // tensor-core error flag (device)
 };
@@ -35,6 +36,10 @@ cudaError_t init(Work* w, void* mem, int64_t nmax, int* err, cudaStream_t st);
 // strict upper triangle is not touched.  *info (device) becomes k + 1 for the
 // first pivot k that is not positive and finite, else 0 (LAPACK potrf).
 cudaError_t potrf(Work& w, int n, double* A, int64_t lda, int* info, tcg::Mode mode, cudaStream_t st,
+                  int64_t* launches);
+// x <- (L L')^-1 x with the factor of the last potrf of this workspace (the
+// inverses of its diagonal blocks are kept); nothing is done when *info != 0.
+cudaError_t solve(const Work& w, int n, const double* L, int64_t ld, double* x, const int* info, cudaStream_t st,
                   int64_t* launches);
 
 }  // namespace chol

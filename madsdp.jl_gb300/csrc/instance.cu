@@ -409,7 +409,15 @@ struct msdp_solver {
   int64_t tfix_len = 0;
   int* terr = nullptr;
   int64_t tc_products = 0;  // tensor-core products issued
-  chol::Work cw;            // blocked Cholesky (Schur matrix and blocks)
+  chol::Work cw, cwH;       // blocked Cholesky: blocks, and the Schur matrix (kept for its solves)
+  int* hinfo_dev = nullptr; // status of the Schur factor
+  // mixed precision: split-precision assembly and FP32-class factor with
+  // FP64 iterative refinement while `mixed_on`; FP64 after a stall
+  bool mixed_on = false;
+  double reg_used = 0.0;
+  double *ir_r = nullptr, *ir_d = nullptr, *ir_h = nullptr;
+  int n32 = 0, n64 = 0;            // iterations by Schur precision
+  int64_t ir_steps = 0, ir_fallbacks = 0;
   double* work = nullptr;
   int lwork = 0;
   double *lq = nullptr, *lh = nullptr;  // Lanczos basis (n x (kLanczosMax + 1)) and projections
@@ -586,10 +594,12 @@ void syrk(S* s, bool trans, int n, int k, double alpha, const double* A, int lda
   tc_product(s, s->tA, s->tA, tcg::kFp64, C, ldc, alpha, beta, true);
 }
 
-// potrf of the lower triangle in place (chol.h); returns the info index
-int potrf(S* s, int n, double* A, int lda, tcg::Mode mode = tcg::kFp64) {
+// potrf of the lower triangle of an n x n block in place (chol.h); returns
+// the info index
+int potrf(S* s, int n, double* A, int lda) {
   const int k = next_info(s);
-  note(s, chol::potrf(s->cw, n, A, lda, s->dinfo + k, mode, s->st, &s->launches) == cudaSuccess, "chol::potrf");
+  note(s, chol::potrf(s->cw, n, A, lda, s->dinfo + k, tcg::kFp64, s->st, &s->launches) == cudaSuccess,
+       "chol::potrf");
   return k;
 }
 
@@ -845,13 +855,16 @@ void schur_complement(S* s, double* H, tcg::Mode mode) {
   }
 }
 
-// Regularization retry loop (src/solver.jl:299-314, src/schur_solvers.jl:15-19)
-bool factorize_schur(S* s, bool* ok) {
+// Regularization retry loop (src/solver.jl:299-314, src/schur_solvers.jl:15-19).
+// kMixed: split-precision assembly and an FP32-class factor (the solve is
+// refined in FP64, solve_schur); when that factorization breaks down, the
+// FP64 Schur matrix is used from then on.
+bool factorize_schur(S* s, bool* ok, tcg::Mode mode) {
   const int m = s->m;
   *ok = false;
   if (m == 0) { *ok = true; return true; }
   mark(s, PH_ASSEMBLY);
-  schur_complement(s, s->H0, tcg::kFp64);
+  schur_complement(s, s->H0, mode);
   mark(s, PH_FACTOR);
   double reg = s->opt.regularize_schur;
   for (int t = 0; t < s->opt.max_schur_reg; ++t) {
@@ -859,16 +872,106 @@ bool factorize_schur(S* s, bool* ok) {
     CU(s, cudaMemcpyAsync(s->H, s->H0, sizeof(double) * m * m, cudaMemcpyDeviceToDevice, s->st));
     if (reg > 0) LAUNCH(s, k_add_diag, m, m, s->H, (int64_t)m, reg);
     const int nf = reduce(s, RED_NONFINITE, (int64_t)m * m, s->H);
-    const int k = potrf(s, m, s->H, m);
+    note(s, chol::potrf(s->cwH, m, s->H, m, s->hinfo_dev, mode, s->st, &s->launches) == cudaSuccess, "chol::potrf");
+    const int k = next_info(s);
+    CU(s, cudaMemcpyAsync(s->dinfo + k, s->hinfo_dev, sizeof(int), cudaMemcpyDeviceToDevice, s->st));
     if (!fetch(s)) return false;
-    if (s->hinfo[k] == 0 && s->hslots[nf] == 0.0) { *ok = true; return true; }
+    if (s->hinfo[k] == 0 && s->hslots[nf] == 0.0) {
+      s->reg_used = reg;
+      *ok = true;
+      return true;
+    }
+    if (mode == tcg::kMixed) {
+      s->mixed_on = false;
+      s->ir_fallbacks += 1;
+      return factorize_schur(s, ok, tcg::kFp64);
+    }
     reg = reg == 0.0 ? 1e-12 : 10.0 * reg;
   }
   return true;
 }
+bool factorize_schur(S* s, bool* ok) { return factorize_schur(s, ok, s->mixed_on ? tcg::kMixed : tcg::kFp64); }
 
-// ---- directions (src/step.jl:63-124)
-void solve_directions(S* s, double mu, bool corrected) {
+// out = L^-T L^-1 v with the Cholesky factor in H (chol.h)
+void chol_solve(S* s, const double* v, double* out) {
+  const int m = s->m;
+  if (out != v) CU(s, cudaMemcpyAsync(out, v, sizeof(double) * m, cudaMemcpyDeviceToDevice, s->st));
+  note(s, chol::solve(s->cwH, m, s->H, m, out, s->hinfo_dev, s->st, &s->launches) == cudaSuccess, "chol::solve");
+}
+
+// out = (H + reg I) v in FP64 without forming H: sum over blocks of
+// A(E(A*(v))) plus C_lin diag(x/z) C_lin' v (the definition of the Schur
+// complement, src/solver.jl:30-31,117-118; NT, where H is symmetric).
+// The blocks' T1/T2 temporaries are free between the rhs and the directions.
+void schur_apply(S* s, const double* v, double* out) {
+  const int m = s->m, ns = s->ns;
+  CU(s, cudaMemsetAsync(out, 0, sizeof(double) * m, s->st));
+  for (auto& b : s->B) {
+    jtprod(s, b, v, b.T1);
+    apply_E(s, b, b.T1, b.T2);
+    jprod(s, b, b.T2, out, true);
+  }
+  if (ns) {
+    k_gemv_t<<<std::min(ns, 152 * 16), kThreads, 0, s->st>>>(m, ns, s->Clin, m, v, s->ctv, 0);
+    s->launches += 1;
+    LAUNCH(s, k_mul, ns, ns, s->ctv, s->wlin, s->vlin);
+    LAUNCH(s, k_gemv_n, m, m, ns, s->Clin, (int64_t)m, s->vlin, out, 1);
+  }
+  if (s->reg_used > 0.0) LAUNCH(s, k_lin, m, m, out, 1.0, out, s->reg_used, v, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+}
+
+constexpr int kMaxRefine = 10;
+
+// dy = (H + reg I)^-1 h.  FP64: two triangular solves with the factor.
+// Mixed: the FP32-class factor's solution refined with FP64 residuals
+// h - (H + reg I) dy of the matrix-free operator until the residual stops
+// shrinking; if it then exceeds 1e-11 |h|, the Schur matrix is assembled
+// and factored in FP64 for this and every later iteration.
+bool solve_schur(S* s, bool* ok) {
+  const int m = s->m;
+  *ok = true;
+  chol_solve(s, s->h, s->dy);
+  if (!s->mixed_on) return !s->fail;
+  CU(s, cudaMemcpyAsync(s->ir_h, s->h, sizeof(double) * m, cudaMemcpyDeviceToDevice, s->st));
+  reset_slots(s);
+  const int hs = reduce(s, RED_MAXABS, m, s->ir_h);
+  if (!fetch(s)) return false;
+  const double hn = std::max(s->hslots[hs], 1e-300);
+  double prev = INFINITY, rn = INFINITY;
+  int it = 0;
+  for (; it < kMaxRefine; ++it) {
+    schur_apply(s, s->dy, s->ir_r);
+    LAUNCH(s, k_lin, m, m, s->ir_r, 1.0, s->ir_h, -1.0, s->ir_r, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+    reset_slots(s);
+    const int rs = reduce(s, RED_MAXABS, m, s->ir_r);
+    if (!fetch(s)) return false;
+    rn = s->hslots[rs];
+    if (!(rn <= 1e-14 * hn) && rn < 0.5 * prev) {
+      prev = rn;
+      chol_solve(s, s->ir_r, s->ir_d);
+      LAUNCH(s, k_lin, m, m, s->dy, 1.0, s->dy, 1.0, s->ir_d, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
+      continue;
+    }
+    break;
+  }
+  s->ir_steps += it;
+  if (std::isfinite(rn) && rn <= 1e-11 * hn) return true;
+  // refinement stalled: FP64 Schur matrix from now on
+  s->mixed_on = false;
+  s->ir_fallbacks += 1;
+  bool f = false;
+  if (!factorize_schur(s, &f, tcg::kFp64)) return false;
+  if (!f) {
+    *ok = false;
+    return true;
+  }
+  chol_solve(s, s->ir_h, s->dy);
+  CU(s, cudaMemcpyAsync(s->h, s->ir_h, sizeof(double) * m, cudaMemcpyDeviceToDevice, s->st));
+  return !s->fail;
+}
+
+// ---- directions (src/step.jl:63-124); false on a CUDA/library failure
+bool solve_directions(S* s, double mu, bool corrected) {
   const int m = s->m, ns = s->ns;
   // rhs
   if (m) CU(s, cudaMemcpyAsync(s->h, s->Rp, sizeof(double) * m, cudaMemcpyDeviceToDevice, s->st));
@@ -884,9 +987,12 @@ void solve_directions(S* s, double mu, bool corrected) {
   }
   // dely = H^-1 h
   if (m) {
-    CU(s, cudaMemcpyAsync(s->dy, s->h, sizeof(double) * m, cudaMemcpyDeviceToDevice, s->st));
-    CB(s, cublasDtrsv(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, m, s->H, m, s->dy, 1));
-    CB(s, cublasDtrsv(s->cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, m, s->H, m, s->dy, 1));
+    bool ok = true;
+    if (!solve_schur(s, &ok)) return false;
+    if (!ok) {
+      s->status = MSDP_ERROR_IN_STEP_COMPUTATION;
+      return true;
+    }
   }
   // directions
   for (auto& b : s->B) {
@@ -907,6 +1013,7 @@ void solve_directions(S* s, double mu, bool corrected) {
     }
     LAUNCH(s, k_dir_lin, ns, ns, mu, s->Rdlin, s->ctv, s->x, s->zinv, corrected ? s->corrlin : nullptr, s->dz, s->dx);
   }
+  return !s->fail;
 }
 
 // ---- Mehrotra correction (src/step.jl:128-136, src/directions.jl:90-100,123-127)
@@ -1172,7 +1279,8 @@ bool iterate_mehrotra(S* s) {
   const double mu = tc / std::max(nu(s), 1);
   s->mu = mu;
   mark(s, PH_DIRECTIONS);
-  solve_directions(s, 0.0, false);
+  if (!solve_directions(s, 0.0, false)) return false;
+  if (s->status != MSDP_REGULAR) return true;
   double aa = 0, ba = 0, mua = 0;
   mark(s, PH_STEP);
   if (!step_lengths(s, &aa, &ba) || !affine_complementarity(s, aa, ba, &mua)) return false;
@@ -1181,12 +1289,14 @@ bool iterate_mehrotra(S* s) {
   mark(s, PH_CORRECTION);
   correction(s);
   mark(s, PH_DIRECTIONS);
-  solve_directions(s, sigma * mu, true);
+  if (!solve_directions(s, sigma * mu, true)) return false;
+  if (s->status != MSDP_REGULAR) return true;
   double a = 0, bt = 0;
   mark(s, PH_STEP);
   if (!step_lengths(s, &a, &bt)) return false;
   mark(s, PH_STEP_UPDATE);
   const bool r = take_step(s, a, bt);
+  (s->mixed_on ? s->n32 : s->n64) += 1;
   collect_marks(s);
   return r;
 }
@@ -1196,9 +1306,11 @@ bool iterate_adaptive(S* s) {
   bool ok = false;
   if (!start_iteration(s, &ok)) return false;
   if (!ok) return true;
-  solve_directions(s, s->mu, false);
+  if (!solve_directions(s, s->mu, false)) return false;
+  if (s->status != MSDP_REGULAR) return true;
   double a = 0, bt = 0;
   if (!step_lengths(s, &a, &bt) || !take_step(s, a, bt)) return false;
+  (s->mixed_on ? s->n32 : s->n64) += 1;
   double tc = 0.0;
   if (!total_complementarity(s, &tc)) return false;
   double mu = s->comp.ratio * tc / std::max(nu(s), 1);
@@ -1340,9 +1452,13 @@ int tc_setup(S* s, bool mixed) {
   s->tfix = (long long*)tcalloc(8 * fixn);
   s->tfix_len = fixn;
   s->terr = (int*)tcalloc(sizeof(int));
-  void* cwm = tcalloc(chol::work_bytes(std::max(nmax, m)));
-  if (!s->tAm || !s->tBm || !s->tfix || !s->terr || !cwm) return 1;
-  CU(s, chol::init(&s->cw, cwm, std::max(nmax, m), s->terr, s->st));
+  void* cwm = tcalloc(chol::work_bytes(nmax));
+  void* cwh = tcalloc(chol::work_bytes(std::max(m, 1)));
+  s->hinfo_dev = (int*)tcalloc(sizeof(int));
+  if (!s->tAm || !s->tBm || !s->tfix || !s->terr || !cwm || !cwh || !s->hinfo_dev) return 1;
+  CU(s, chol::init(&s->cw, cwm, nmax, s->terr, s->st));
+  CU(s, chol::init(&s->cwH, cwh, std::max(m, 1), s->terr, s->st));
+  CU(s, cudaMemsetAsync(s->hinfo_dev, 0, sizeof(int), s->st));
   // the constraint data went up by synchronous copies from pageable memory
   CU(s, cudaDeviceSynchronize());
   CU(s, cudaMemsetAsync(s->terr, 0, sizeof(int), s->st));
@@ -1419,8 +1535,11 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   if (opt) o = *opt; else msdp_default_options(&o);
   if (d->nblocks < 0 || d->m < 0 || d->ns < 0 || (d->nblocks == 0 && d->ns == 0)) return MSDP_ERR_INVALID_ARGUMENT;
   if (c.algorithm != MSDP_PRIMAL_DUAL || c.schur != MSDP_DENSE_CHOLESKY ||
-      (c.precision != MSDP_FP64 && c.precision != MSDP_FP64_TENSOR))
+      (c.precision != MSDP_FP64 && c.precision != MSDP_FP64_TENSOR && c.precision != MSDP_MIXED))
     return MSDP_ERR_UNSUPPORTED;
+  // mixed: the refinement applies H matrix-free, which equals the factored
+  // lower-triangle matrix only when H is symmetric (NT)
+  if (c.precision == MSDP_MIXED && c.direction != MSDP_NT) return MSDP_ERR_UNSUPPORTED;
   if (!(c.tau > 0.0) || !(c.shrink > 0.0 && c.shrink < 1.0) || !(c.boundary > 0.0 && c.boundary <= 1.0) ||
       o.max_iter < 0 || (c.initial_point == MSDP_DUAL_SHIFT && !(c.initial_shift > 0.0)))
     return MSDP_ERR_INVALID_ARGUMENT;
@@ -1473,12 +1592,14 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   s->x = vec(ns); s->z = vec(ns); s->dx = vec(ns); s->dz = vec(ns); s->Rdlin = vec(ns); s->zinv = vec(ns);
   s->corrlin = vec(ns); s->vlin = vec(ns); s->ctv = vec(ns); s->wlin = vec(ns);
   s->H = vec((int64_t)m * m); s->H0 = vec((int64_t)m * m);
+  s->ir_r = vec(m); s->ir_d = vec(m); s->ir_h = vec(m);
   if (dense_ws) { s->Tb = vec(dense_ws); s->Bb = vec(dense_ws); }
   s->partial = vec(kRedBlocks); s->slots = vec(kSlots);
   s->dinfo = dalloc<int>(s, kInfos);
   bool okalloc = s->b && s->dlin && s->Clin && s->Cw && s->y && s->dy && s->Rp && s->h && s->acc && s->x && s->z &&
                  s->dx && s->dz && s->Rdlin && s->zinv && s->corrlin && s->vlin && s->ctv && s->wlin && s->H &&
-                 s->H0 && s->partial && s->slots && s->dinfo && (!dense_ws || (s->Tb && s->Bb));
+                 s->H0 && s->partial && s->slots && s->dinfo && (!dense_ws || (s->Tb && s->Bb)) && s->ir_r &&
+                 s->ir_d && s->ir_h;
   if (!okalloc) return bail(MSDP_ERR_OUT_OF_MEMORY);
   if (cudaMallocHost((void**)&s->hslots, sizeof(double) * kSlots) != cudaSuccess ||
       cudaMallocHost((void**)&s->hinfo, sizeof(int) * kInfos) != cudaSuccess)
@@ -1625,6 +1746,10 @@ int msdp_solver_solve(msdp_solver* s) {
   if (!s) return MSDP_ERR_INVALID_ARGUMENT;
   s->fail = 0;
   for (auto& v : s->phase_s) v = 0.0;
+  s->mixed_on = s->comp.precision == MSDP_MIXED;
+  s->n32 = s->n64 = 0;
+  s->ir_steps = s->ir_fallbacks = 0;
+  s->reg_used = 0.0;
   const double t0 = now_s();
   int rc = initialize(s);
   if (rc) return rc;
@@ -1642,7 +1767,7 @@ int msdp_solver_solve(msdp_solver* s) {
 int msdp_solver_get_stats(const msdp_solver* s, msdp_stats* o) {
   if (!s || !o) return MSDP_ERR_INVALID_ARGUMENT;
   std::memset(o, 0, sizeof(*o));
-  o->status = s->status; o->iter = s->iter; o->iter_fp64 = s->iter; o->iter_fp32 = 0;
+  o->status = s->status; o->iter = s->iter; o->iter_fp64 = s->n64; o->iter_fp32 = s->n32;
   o->pobj = s->pobj; o->dobj = s->dobj; o->inf_pr = s->inf_pr; o->inf_du = s->inf_du; o->gap = s->gap;
   o->mu = s->mu; o->sigma = s->sigma; o->alpha = s->alpha; o->beta = s->beta; o->solve_ns = s->solve_s * 1e9;
   return MSDP_OK;
@@ -1658,6 +1783,95 @@ int msdp_solver_get_solution(msdp_solver* s, double* const* X, double* y, double
   if (z && s->ns) CU(s, cudaMemcpyAsync(z, s->z, 8 * s->ns, cudaMemcpyDeviceToHost, s->st));
   CU(s, cudaStreamSynchronize(s->st));
   return s->fail;
+}
+
+// ---- component-granular calls (one GPU component beside CPU components)
+int msdp_solver_set_iterate(msdp_solver* s, const double* const* X, const double* const* Sm, const double* y,
+                            const double* x, const double* z) {
+  if (!s || (s->nb && (!X || !Sm)) || (s->m && !y) || (s->ns && (!x || !z))) return MSDP_ERR_INVALID_ARGUMENT;
+  s->fail = 0;
+  for (int i = 0; i < s->nb; ++i) {
+    if (!X[i] || !Sm[i]) return MSDP_ERR_INVALID_ARGUMENT;
+    const int64_t nn = (int64_t)s->B[i].n * s->B[i].n;
+    CU(s, cudaMemcpyAsync(s->B[i].X, X[i], 8 * nn, cudaMemcpyHostToDevice, s->st));
+    CU(s, cudaMemcpyAsync(s->B[i].S, Sm[i], 8 * nn, cudaMemcpyHostToDevice, s->st));
+  }
+  if (s->m) CU(s, cudaMemcpyAsync(s->y, y, 8 * s->m, cudaMemcpyHostToDevice, s->st));
+  if (s->ns) {
+    CU(s, cudaMemcpyAsync(s->x, x, 8 * s->ns, cudaMemcpyHostToDevice, s->st));
+    CU(s, cudaMemcpyAsync(s->z, z, 8 * s->ns, cudaMemcpyHostToDevice, s->st));
+  }
+  s->status = MSDP_REGULAR;
+  if (!update_residuals(s)) return s->fail ? s->fail : MSDP_ERR_CUDA;
+  return s->fail;
+}
+
+int msdp_solver_prepare(msdp_solver* s, int32_t* ok) {
+  if (!s || !ok) return MSDP_ERR_INVALID_ARGUMENT;
+  s->fail = 0;
+  bool p = false;
+  if (!prepare(s, &p)) return s->fail ? s->fail : MSDP_ERR_CUDA;
+  *ok = p ? 1 : 0;
+  return MSDP_OK;
+}
+
+int msdp_solver_schur_assemble(msdp_solver* s, int32_t precision, double* H) {
+  if (!s || (s->m && !H) || (precision != MSDP_FP64 && precision != MSDP_MIXED)) return MSDP_ERR_INVALID_ARGUMENT;
+  if (precision == MSDP_MIXED && !is_nt(s)) return MSDP_ERR_UNSUPPORTED;
+  if (precision == MSDP_MIXED &&
+      std::any_of(s->B.begin(), s->B.end(), [](const Blk& b) { return b.dense && !b.stk[1].s; }))
+    return MSDP_ERR_UNSUPPORTED;  // split-precision slices are made for mixed-precision solvers only
+  s->fail = 0;
+  if (!s->m) return MSDP_OK;
+  schur_complement(s, s->H0, precision == MSDP_MIXED ? tcg::kMixed : tcg::kFp64);
+  CU(s, cudaMemcpyAsync(H, s->H0, 8 * (int64_t)s->m * s->m, cudaMemcpyDeviceToHost, s->st));
+  CU(s, cudaStreamSynchronize(s->st));
+  return s->fail;
+}
+
+int msdp_solver_get_block_matrix(msdp_solver* s, int32_t block, int32_t which, double* out) {
+  if (!s || !out || block < 0 || block >= s->nb) return MSDP_ERR_INVALID_ARGUMENT;
+  Blk& b = s->B[block];
+  const double* src = nullptr;
+  int64_t len = (int64_t)b.n * b.n;
+  switch (which) {
+    case MSDP_SMAT_W: src = b.W; break;
+    case MSDP_SMAT_G: src = b.G; break;
+    case MSDP_SMAT_SINV: src = b.Si; break;
+    case MSDP_SMAT_LS: src = b.Ls; break;
+    case MSDP_SMAT_LX: src = b.Lx; break;
+    case MSDP_SMAT_D: src = b.D; len = b.n; break;
+    default: return MSDP_ERR_INVALID_ARGUMENT;
+  }
+  s->fail = 0;
+  CU(s, cudaMemcpyAsync(out, src, 8 * len, cudaMemcpyDeviceToHost, s->st));
+  CU(s, cudaStreamSynchronize(s->st));
+  return s->fail;
+}
+
+int msdp_solver_step_eig(msdp_solver* s, int32_t block, const double* L, const double* D, double* lambda_min) {
+  if (!s || !L || !D || !lambda_min || block < 0 || block >= s->nb) return MSDP_ERR_INVALID_ARGUMENT;
+  Blk& b = s->B[block];
+  const int n = b.n;
+  const int64_t nn = (int64_t)n * n;
+  s->fail = 0;
+  reset_slots(s);
+  CU(s, cudaMemcpyAsync(b.T3, L, 8 * nn, cudaMemcpyHostToDevice, s->st));
+  CU(s, cudaMemcpyAsync(b.T2, D, 8 * nn, cudaMemcpyHostToDevice, s->st));
+  form_congruence(s, n, b.T3, b.T2, b.T1);
+  int slot;
+  if (n <= kLanczosWarpMax) {
+    slot = s->nslot++;
+    LanczosJob job{n, b.T1, s->lq2, s->lw2, s->slots + slot};
+    CU(s, cudaMemcpyAsync(s->ljobs, &job, sizeof(job), cudaMemcpyHostToDevice, s->st));
+    k_lanczos_batched<<<1, 32, 0, s->st>>>((const LanczosJob*)s->ljobs);
+    s->launches += 1;
+  } else {
+    slot = eigmin_large(s, b, b.T1);
+  }
+  if (!fetch(s)) return s->fail ? s->fail : MSDP_ERR_CUDA;
+  *lambda_min = s->hslots[slot];
+  return MSDP_OK;
 }
 
 int msdp_solver_get_trajectory(const msdp_solver* s, msdp_iter_record* out, int32_t capacity, int32_t* count) {

@@ -8,11 +8,12 @@ from .components import (AdaptiveMu, CholeskyBacktrack, DenseCholesky, DualCente
                          EigenStep, HKM, InitialPoint, MadNLPSchur, Mehrotra, NT, Options,
                          PrimalDual, QRSchur, ScaledIdentity, Status)
 from .model import BlockConstraints, Model
-from .solver import Batch, Context, GPUError, InstanceSolver, MadSDPSolver, default_context, madsdp
+from .solver import (Batch, Context, GPUError, InstanceSolver, MadSDPSolver, SchurWorkspace, default_context,
+                     madsdp)
 
 __all__ = [
     "AdaptiveMu", "Batch", "BlockConstraints", "CholeskyBacktrack", "Context", "DenseCholesky",
     "DualCentering", "DualShift", "EigenStep", "GPUError", "HKM", "InitialPoint", "InstanceSolver", "MadNLPSchur",
-    "MadSDPSolver", "Mehrotra", "Model", "NT", "Options", "PrimalDual", "QRSchur",
+    "SchurWorkspace", "MadSDPSolver", "Mehrotra", "Model", "NT", "Options", "PrimalDual", "QRSchur",
     "ScaledIdentity", "Status", "default_context", "madsdp",
 ]

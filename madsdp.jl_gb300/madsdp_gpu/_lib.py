@@ -117,6 +117,16 @@ SIGNATURES = [
     ("msdp_solver_profile_field_name", C.c_char_p, [i32]),
     ("msdp_solver_launch_count", i64, [C.c_void_p]),
     ("msdp_solver_last_error", C.c_char_p, [C.c_void_p]),
+    ("msdp_solver_set_iterate", i32, [C.c_void_p, P(P(f64)), P(P(f64)), P(f64), P(f64), P(f64)]),
+    ("msdp_solver_prepare", i32, [C.c_void_p, P(i32)]),
+    ("msdp_solver_schur_assemble", i32, [C.c_void_p, i32, P(f64)]),
+    ("msdp_solver_get_block_matrix", i32, [C.c_void_p, i32, i32, P(f64)]),
+    ("msdp_solver_step_eig", i32, [C.c_void_p, i32, P(f64), P(f64), P(f64)]),
+    ("msdp_schur_create", i32, [C.c_void_p, i32, i32, P(C.c_void_p)]),
+    ("msdp_schur_destroy", i32, [C.c_void_p]),
+    ("msdp_schur_factorize", i32, [C.c_void_p, P(f64), P(i32)]),
+    ("msdp_schur_solve", i32, [C.c_void_p, P(f64)]),
+    ("msdp_schur_fp64_active", i32, [C.c_void_p]),
     ("msdp_dense_cholesky", i32, [i32, i32, C.c_void_p, i64, P(i32), C.c_void_p]),
     ("msdp_tc_gemm", i32, [i32, i32, i32, i64, i64, i64, f64, C.c_void_p, i64, C.c_void_p, i64, f64, C.c_void_p, i64,
                            i32, C.c_void_p]),

@@ -507,7 +507,8 @@ class InstanceSolver:
         h = C.c_void_p()
         rc = self.lib.msdp_solver_create(self.ctx.h, C.byref(mm.desc), C.byref(comp), C.byref(opts), C.byref(h))
         if rc == -4:
-            raise NotImplementedError("the whole-GPU solver runs PrimalDual with DenseCholesky in FP64")
+            raise NotImplementedError("the whole-GPU solver runs PrimalDual with DenseCholesky, in FP64 or, "
+                                      "with the NT direction, in mixed precision")
         if rc != 0:
             raise (ValueError if rc == -1 else GPUError)(f"msdp_solver_create: {_lib.ERRORS.get(rc, rc)}")
         self.h = h
@@ -563,6 +564,61 @@ class InstanceSolver:
         self.lib.msdp_solver_get_stats(self.h, C.byref(st))
         return _stats_dict(st)
 
+    # --- component-granular calls (src/primal_dual.jl:29-37, solver.jl:304, step.jl:150-183)
+    MATRICES = {"W": 0, "G": 1, "Sinv": 2, "Ls": 3, "Lx": 4, "D": 5}
+
+    def set_iterate(self, X, S, y, x=None, z=None):
+        """Load an iterate of the host driver (and update the residuals)."""
+        m = self.model
+        Xs = [np.asfortranarray(np.asarray(a, dtype=np.float64)) for a in X]
+        Ss = [np.asfortranarray(np.asarray(a, dtype=np.float64)) for a in S]
+        Xp = (f64p * max(len(Xs), 1))(*[_ptr(a) for a in Xs])
+        Sp = (f64p * max(len(Ss), 1))(*[_ptr(a) for a in Ss])
+        yv = np.ascontiguousarray(y, dtype=np.float64)
+        xv = np.ascontiguousarray(np.zeros(m.ns) if x is None else x, dtype=np.float64)
+        zv = np.ascontiguousarray(np.zeros(m.ns) if z is None else z, dtype=np.float64)
+        rc = self.lib.msdp_solver_set_iterate(self.h, Xp, Sp, _ptr(yv), _ptr(xv), _ptr(zv))
+        if rc != 0:
+            raise GPUError(f"msdp_solver_set_iterate: {_lib.ERRORS.get(rc, rc)}")
+
+    def prepare(self) -> bool:
+        """_prepare!: Cholesky of S, S^-1, NT scaling, Cholesky of X."""
+        ok = C.c_int32()
+        rc = self.lib.msdp_solver_prepare(self.h, C.byref(ok))
+        if rc != 0:
+            raise GPUError(f"msdp_solver_prepare: {_lib.ERRORS.get(rc, rc)}")
+        return bool(ok.value)
+
+    def schur_assemble(self, precision: str = "fp64") -> np.ndarray:
+        """The Schur complement matrix of the prepared scaling (lower triangle)."""
+        m = self.model.m
+        H = np.zeros((m, m), order="F")
+        code = {"fp64": 0, "mixed": 1}[precision]
+        rc = self.lib.msdp_solver_schur_assemble(self.h, code, _ptr(H))
+        if rc == -4:
+            raise NotImplementedError("split-precision assembly needs an NT solver created in mixed precision")
+        if rc != 0:
+            raise GPUError(f"msdp_solver_schur_assemble: {_lib.ERRORS.get(rc, rc)}")
+        return np.tril(H)
+
+    def block_matrix(self, block: int, which: str) -> np.ndarray:
+        n = self.model.sides[block]
+        out = np.zeros(n) if which == "D" else np.zeros((n, n), order="F")
+        rc = self.lib.msdp_solver_get_block_matrix(self.h, block, self.MATRICES[which], _ptr(out))
+        if rc != 0:
+            raise GPUError(f"msdp_solver_get_block_matrix: {_lib.ERRORS.get(rc, rc)}")
+        return out
+
+    def step_eig(self, block: int, L, D) -> float:
+        """lambda_min(L^-1 D L^-T) (EigenStep, src/step.jl:150-183)."""
+        Lf = np.asfortranarray(L, dtype=np.float64)
+        Df = np.asfortranarray(D, dtype=np.float64)
+        lam = C.c_double()
+        rc = self.lib.msdp_solver_step_eig(self.h, block, _ptr(Lf), _ptr(Df), C.byref(lam))
+        if rc != 0:
+            raise GPUError(f"msdp_solver_step_eig: {_lib.ERRORS.get(rc, rc)}")
+        return lam.value
+
     def solution(self):
         m = self.model
         X = [np.zeros((n, n), order="F") for n in m.sides]
@@ -579,6 +635,57 @@ class InstanceSolver:
         cnt = C.c_int32()
         self.lib.msdp_solver_get_trajectory(self.h, arr, cap, C.byref(cnt))
         return [{k: getattr(r, k) for k, _ in _lib.IterRecord._fields_} for r in arr[:min(cnt.value, cap)]]
+
+
+class SchurWorkspace:
+    """A Schur-solver component on the GPU (src/components.jl:253-266):
+    schur_workspace(DenseCholesky(), Float64, m), factorize!(ws) of a
+    host-assembled H, schur_solve!(ws, rhs).  precision "mixed": FP32-class
+    factor refined in FP64 against H, FP64 after a stalled refinement or a
+    breakdown of the FP32-class factorization."""
+
+    def __init__(self, m: int, precision: str = "fp64", context: Optional[Context] = None):
+        self.ctx = context or default_context()
+        self.lib = self.ctx.lib
+        self.m = int(m)
+        h = C.c_void_p()
+        rc = self.lib.msdp_schur_create(self.ctx.h, self.m, {"fp64": 0, "mixed": 1}[precision], C.byref(h))
+        if rc != 0:
+            raise GPUError(f"msdp_schur_create: {_lib.ERRORS.get(rc, rc)}")
+        self.h = h
+        self.ctx.adopt(self)
+
+    def factorize(self, H) -> bool:
+        Hf = np.asfortranarray(H, dtype=np.float64)
+        if Hf.shape != (self.m, self.m):
+            raise ValueError("H must be m x m")
+        ok = C.c_int32()
+        rc = self.lib.msdp_schur_factorize(self.h, _ptr(Hf), C.byref(ok))
+        if rc != 0:
+            raise GPUError(f"msdp_schur_factorize: {_lib.ERRORS.get(rc, rc)}")
+        return bool(ok.value)
+
+    def solve(self, rhs) -> np.ndarray:
+        x = np.array(rhs, dtype=np.float64, copy=True)
+        rc = self.lib.msdp_schur_solve(self.h, _ptr(x))
+        if rc != 0:
+            raise GPUError(f"msdp_schur_solve: {_lib.ERRORS.get(rc, rc)}")
+        return x
+
+    @property
+    def fp64_active(self) -> bool:
+        return bool(self.lib.msdp_schur_fp64_active(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.msdp_schur_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _use_instance_engine(model: Model) -> bool:
@@ -603,9 +710,12 @@ class MadSDPSolver:
             # the whole-GPU engine runs PrimalDual + DenseCholesky in FP64
             schur = kwargs.get("schur")
             prec = kwargs.get("precision", "fp64")
-            supported = (not isinstance(kwargs.get("algorithm"), DualCentering)
+            alg = kwargs.get("algorithm")
+            direction = kwargs.get("direction") or (alg.direction if isinstance(alg, PrimalDual) else None)
+            supported = (not isinstance(alg, DualCentering)
                          and (schur is None or isinstance(schur, DenseCholesky))
-                         and prec in ("fp64", "fp64_tensor"))
+                         and (prec in ("fp64", "fp64_tensor")
+                              or (prec == "mixed" and (direction is None or isinstance(direction, NT)))))
             engine = "instance" if supported and (prec == "fp64_tensor" or _use_instance_engine(model)) else "batch"
         self.engine = engine
         self.batch = Batch([model], **kwargs) if engine == "batch" else None

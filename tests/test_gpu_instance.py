@@ -135,7 +135,7 @@ def test_auto_engine_and_unsupported(gpu_ctx):
     with pytest.raises(NotImplementedError):
         M.InstanceSolver(g.maxcut(30, 0.2, seed=1), schur=M.QRSchur())
     with pytest.raises(NotImplementedError):
-        M.InstanceSolver(g.maxcut(30, 0.2, seed=1), precision="mixed")
+        M.InstanceSolver(g.maxcut(30, 0.2, seed=1), precision="mixed", direction=M.HKM())
     with pytest.raises(NotImplementedError):
         M.Batch([g.maxcut(30, 0.2, seed=1)], precision="fp64_tensor")
 
@@ -151,16 +151,22 @@ def test_config2_maxcut_n2000_matches_oracle(gpu_ctx):
     assert_matches_oracle(s, ref)
 
 
-def test_config3_dense_mixed_cones_full_size(gpu_ctx):
+@pytest.fixture(scope="module")
+def config3():
+    model = g.dense_random([200, 100, 50, 50], 500, 2000, seed=4)
+    return model, o.Solver(model).solve()
+
+
+def test_config3_dense_mixed_cones_full_size(gpu_ctx, config3):
     """Blocks [200, 100, 50, 50] + 500 scalars, m = 2000, dense A
     (configuration 3) at full size: NT matches the oracle (iterations,
     objectives, per-iteration trajectory; the oracle assembles the dense
     Schur matrix by batched dense products, about a minute on the host
     cores).  Size-independent checks besides: NT and HKM both reach 1e-7,
     their objectives agree, and the solution is in the cones."""
-    model = g.dense_random([200, 100, 50, 50], 500, 2000, seed=4)
+    model, ref = config3
     nt = inst(model)
-    assert_matches_oracle(nt, o.Solver(model).solve())
+    assert_matches_oracle(nt, ref)
     hkm = inst(model, direction=M.HKM())
     for s in (nt, hkm):
         assert s.status == M.Status.SOLVE_SUCCEEDED, s.stats
@@ -172,3 +178,28 @@ def test_config3_dense_mixed_cones_full_size(gpu_ctx):
     for Xi in X:
         assert np.linalg.eigvalsh((Xi + Xi.T) / 2)[0] > -1e-8
     assert np.all(x > -1e-10) and np.all(z > -1e-10)
+
+
+# ---------------------------------------------------------------- mixed precision
+# Split-precision Schur assembly on the tensor cores, FP32-class factor and
+# FP64 iterative refinement against the matrix-free Schur operator, FP64
+# after a stall: same status, objectives to 1e-7 of the oracle's scale and
+# the iteration count within one.
+@pytest.mark.parametrize("model", [g.dense_random([40, 20], 30, 150, seed=2), g.maxcut(120, 0.05, seed=3),
+                                   g.dense_random([60], 0, 400, seed=6)], ids=["dense_scalars", "maxcut", "dense"])
+def test_mixed_instance_matches_oracle(gpu_ctx, model):
+    s = inst(model, precision="mixed")
+    ref = o.Solver(model).solve()
+    assert_matches_oracle(s, ref, traj=False)
+    st = s.stats
+    assert st["iter_fp32"] + st["iter_fp64"] == st["iter"]
+
+
+def test_mixed_config3_full_size(gpu_ctx, config3):
+    """Configuration 3 (NT) in mixed precision: the split-precision
+    assembly and FP32-class factor carry most iterations, and the result
+    equals the FP64 oracle's."""
+    model, ref = config3
+    s = inst(model, precision="mixed")
+    assert_matches_oracle(s, ref, traj=False)
+    assert s.stats["iter_fp32"] >= 1

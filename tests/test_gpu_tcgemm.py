@@ -117,3 +117,29 @@ def test_tc_gemm_rejects_bad_arguments(gpu_ctx):
     assert lib.msdp_tc_gemm(5, 0, 0, 4, 4, 4, 1.0, null, 4, null, 4, 0.0, null, 4, 0, null) == -1
     assert lib.msdp_tc_gemm(0, 0, 0, 4, 3, 4, 1.0, null, 4, null, 4, 0.0, null, 4, 1, null) == -1
     assert lib.msdp_tc_gemm(0, 0, 0, 0, 0, 4, 1.0, null, 4, null, 4, 0.0, null, 1, 0, null) == 0
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 2e-14), (1, 1e-6)])
+def test_tc_gemm_config3_schur_shape(gpu_ctx, prec, tol):
+    """The Schur-complement product of the dense-constraint workload at full
+    size: H = B B' (lower) with B of 2000 rows and K = 20100 (the symmetric
+    vectors of the 200 x 200 block), against a float64 product on the GPU."""
+    import torch
+
+    from madsdp_gpu import _lib
+    lib = _lib.load()
+    m, K = 2000, 20100
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    B = torch.randn(m, K, dtype=torch.float64, device="cuda", generator=gen)  # column-major K x m: op(A) = B
+    Cout = torch.zeros(m, m, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    rc = lib.msdp_tc_gemm(prec, 1, 0, m, m, K, 1.0, C.c_void_p(B.data_ptr()), K, C.c_void_p(B.data_ptr()), K, 0.0,
+                          C.c_void_p(Cout.data_ptr()), m, 1, C.c_void_p(st))
+    assert rc == 0
+    ref = B @ B.T
+    bound = B.abs() @ B.abs().T
+    low = torch.tril(torch.ones(m, m, dtype=torch.bool, device="cuda"))
+    got = Cout.T  # column-major result
+    err = ((got - ref).abs() / bound)[low].max().item()
+    assert err <= tol, err
+    assert (got[~low] == 0).all()
