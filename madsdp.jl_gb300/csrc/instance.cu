@@ -191,13 +191,50 @@ __global__ void k_div_cols(int n, double* G, const double* sc) {
     G[idx] /= sc[idx / n];
 }
 
-// out = diag(sc) V'
-__global__ void k_gi0(int n, const double* V, const double* sc, double* out) {
+// out[i + j n] = Q[j + i n] f[i]: the transpose of Q with its rows scaled
+__global__ void k_scaled_transpose(int n, const double* __restrict__ Q, const double* __restrict__ f,
+                                   double* __restrict__ out) {
   const int64_t nn = (int64_t)n * n;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nn; idx += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(idx % n), j = (int)(idx / n);
-    out[idx] = V[j + (int64_t)i * n] * sc[i];
+    out[idx] = Q[j + (int64_t)i * n] * f[i];
   }
+}
+// f = D^-3/2 = 1 / (D sc)
+__global__ void k_gi_scale(int n, const double* __restrict__ D, const double* __restrict__ sc, double* __restrict__ f) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) f[i] = 1.0 / (D[i] * sc[i]);
+}
+// rows of A scaled: A[i, :] /= sc[i]
+__global__ void k_div_rows(int n, double* A, const double* __restrict__ sc) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nn; idx += (int64_t)gridDim.x * blockDim.x)
+    A[idx] /= sc[idx % n];
+}
+
+// ---- Lanczos steps with the scalars kept on the device
+// w -= a q + b p with a = *pa and b = sqrt(*pbb) (the previous norm squared)
+__global__ void k_lanczos_update(int64_t n, double* __restrict__ w, const double* __restrict__ q,
+                                 const double* __restrict__ p, const double* __restrict__ pa,
+                                 const double* __restrict__ pbb) {
+  const double a = *pa, b = p ? sqrt(*pbb) : 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    w[i] -= a * q[i] + (p ? b * p[i] : 0.0);
+}
+// out[i] -= sum_j A[i + j lda] v[j]
+__global__ void k_gemv_sub(int64_t rows, int cols, const double* __restrict__ A, int64_t lda,
+                           const double* __restrict__ v, double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < cols; ++j) s = fma(A[i + j * lda], v[j], s);
+    out[i] -= s;
+  }
+}
+// out = w / sqrt(*pbb)
+__global__ void k_normalize(int64_t n, const double* __restrict__ w, const double* __restrict__ pbb,
+                            double* __restrict__ out) {
+  const double inv = 1.0 / sqrt(*pbb);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = w[i] * inv;
 }
 
 // out = -(M + M') ./ (D_i + D_j)  (src/directions.jl:90-100)
@@ -314,6 +351,31 @@ __global__ void k_gemv_n(int64_t rows, int cols, const double* __restrict__ A, i
     out[i] = accumulate ? out[i] + s : s;
   }
 }
+// The same for many columns in two passes: partial sums of kGemvChunks
+// column ranges (grid y), then their sum in a fixed order (deterministic).
+constexpr int kGemvChunks = 16;
+__global__ void k_gemv_n_part(int64_t rows, int cols, const double* __restrict__ A, int64_t lda,
+                              const double* __restrict__ v, double* __restrict__ part) {
+  const int per = (cols + kGemvChunks - 1) / kGemvChunks;
+  const int j0 = blockIdx.y * per, j1 = min(cols, j0 + per);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+    double s0 = 0.0, s1 = 0.0;
+    int j = j0;
+    for (; j + 1 < j1; j += 2) {
+      s0 = fma(A[i + j * lda], v[j], s0);
+      s1 = fma(A[i + (j + 1) * lda], v[j + 1], s1);
+    }
+    if (j < j1) s0 = fma(A[i + j * lda], v[j], s0);
+    part[blockIdx.y * rows + i] = s0 + s1;
+  }
+}
+__global__ void k_gemv_n_sum(int64_t rows, const double* __restrict__ part, double* __restrict__ out, int accumulate) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int c = 0; c < kGemvChunks; ++c) s += part[c * rows + i];
+    out[i] = accumulate ? out[i] + s : s;
+  }
+}
 // out[j] (+)= sum_i A[i + j lda] v[i]  (j < cols): one block per column,
 // fixed reduction tree (deterministic)
 __global__ void k_gemv_t(int64_t rows, int cols, const double* __restrict__ A, int64_t lda,
@@ -375,6 +437,10 @@ struct Blk {
   int32_t *erow = nullptr, *ecol = nullptr, *pcon = nullptr;
   double *eval = nullptr, *pval = nullptr;
   double* Aall = nullptr;  // dense: n x (n m), column j*n.. of A_j
+  // NT: Gs = G D^-1/2 and Hx = D^-1/2 Gi for S^-1 = Gs Gs' and the
+  // step-length matrices Hx dX Hx', Gs' dS Gs (orthogonally similar to
+  // Lx^-1 dX Lx^-T and Ls^-1 dS Ls^-T)
+  double *Gs = nullptr, *Hx = nullptr, *gif = nullptr;
   // dense constraints on the tensor cores (sliced once at creation):
   // [A_1; ...; A_m] as rows (j, r) with K = n, in the FP64 (7) and, for the
   // mixed precision, the mixed (3) slicing; HKM also vec(A_j) rows, K = n^2
@@ -400,6 +466,7 @@ struct msdp_solver {
   double *x = nullptr, *z = nullptr, *dx = nullptr, *dz = nullptr, *Rdlin = nullptr, *zinv = nullptr;
   double *corrlin = nullptr, *vlin = nullptr, *ctv = nullptr, *wlin = nullptr;
   double *H = nullptr, *H0 = nullptr, *Tb = nullptr, *Bb = nullptr;
+  double* gpart = nullptr;  // partial sums of the dense A*(y) (kGemvChunks x n^2)
   // tensor-core products: operand slices of the n x n products (tA, tB),
   // the per-iteration operands of the dense assembly (tQ, tS), C_lin and
   // C_lin diag(x/z) (tCl, tCw), the fixed-point workspace and error flag
@@ -576,7 +643,6 @@ tcg::Source op_rows(const double* Mp, int64_t ld, bool trans, int64_t rows, int6
   src.ks = trans ? 1 : ld;
   return src;
 }
-tcg::Mode tc_mode(const S* s) { return s->comp.precision == MSDP_MIXED ? tcg::kMixed : tcg::kFp64; }
 
 // ---- dense linear algebra
 // C = alpha op(A) op(B) + beta C (FP64-accurate tensor-core product)
@@ -635,7 +701,11 @@ void jprod(S* s, Blk& b, const double* X, double* out, bool accumulate) {
 void jtprod(S* s, Blk& b, const double* yv, double* out) {
   const int64_t nn = (int64_t)b.n * b.n;
   if (b.dense) {
-    LAUNCH(s, k_gemv_n, nn, nn, s->m, b.Aall, nn, yv, out, 0);
+    // A*(y) streams all of A: columns split over kGemvChunks block rows
+    const dim3 grid((unsigned)std::min<int64_t>((nn + kThreads - 1) / kThreads, 152 * 8), kGemvChunks);
+    k_gemv_n_part<<<grid, kThreads, 0, s->st>>>(nn, s->m, b.Aall, nn, yv, s->gpart);
+    LAUNCH(s, k_gemv_n_sum, nn, nn, s->gpart, out, 0);
+    s->launches += 1;
   } else {
     LAUNCH(s, k_jtprod, nn, nn, b.posptr, b.pcon, b.pval, yv, out);
   }
@@ -755,30 +825,41 @@ bool prepare(S* s, bool* ok) {
     const int n = b.n;
     const int64_t nn = (int64_t)n * n;
     cs_.push_back(chol_factor(s, n, b.S, b.Ls));
-    // S^-1 from the factor (potri on a copy, lower to full)
-    CU(s, cudaMemcpyAsync(b.Si, b.Ls, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s->st));
-    const int k = next_info(s);
-    CS(s, cusolverDnDpotri(s->cs, CUBLAS_FILL_MODE_LOWER, n, b.Si, n, s->work, s->lwork, s->dinfo + k));
-    LAUNCH(s, k_lower_to_full, nn, n, b.Si);
+    if (!is_nt(s)) {
+      // S^-1 from the factor (potri on a copy, lower to full); NT forms it
+      // from the scaling below
+      CU(s, cudaMemcpyAsync(b.Si, b.Ls, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s->st));
+      const int k = next_info(s);
+      CS(s, cusolverDnDpotri(s->cs, CUBLAS_FILL_MODE_LOWER, n, b.Si, n, s->work, s->lwork, s->dinfo + k));
+      LAUNCH(s, k_lower_to_full, nn, n, b.Si);
+    }
     if (need_lx) cx_.push_back(chol_factor(s, n, b.X, b.Lx));
     if (is_nt(s)) {
       // M = Ls' Lx ; N = M'M ; eig(N) = V diag(lam) V'
       gemm(s, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, 1.0, b.Ls, n, b.Lx, n, 0.0, b.T1, n);
-      const double one = 1.0;
       syrk(s, true, n, n, 1.0, b.T1, n, 0.0, b.T2, n);
       const int ke = next_info(s);
       CS(s, cusolverDnDsyevd(s->cs, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, b.T2, n, b.lam, s->work,
                              s->lwork, s->dinfo + ke));
       lam0.push_back(copy_slot(s, b.lam));
       LAUNCH(s, k_nt_scaling, n, n, b.lam, b.D, b.sc);
-      // G = Lx V diag(sc)^-1 ; Gi = diag(sc) V' Lx^-1 ; W = G G'
+      // G = Lx V D^-1/2 and W = G G'.  From M V = U D (U orthogonal):
+      // Gi = G^-1 = D^-3/2 (M V)' Ls' (no triangular solve) and
+      // S^-1 = G D^-1 G' = Gs Gs' with Gs = G D^-1/2
       gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.Lx, n, b.T2, n, 0.0, b.G, n);
       LAUNCH(s, k_div_cols, nn, n, b.G, b.sc);
-      LAUNCH(s, k_gi0, nn, n, b.T2, b.sc, b.Gi);
-      CB(s, cublasDtrsm(s->cb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
-                        b.Lx, n, b.Gi, n));
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.T1, n, b.T2, n, 0.0, b.T3, n);   // M V
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.Ls, n, b.T3, n, 0.0, b.T1, n);   // Ls M V
+      LAUNCH(s, k_gi_scale, n, n, b.D, b.sc, b.gif);
+      LAUNCH(s, k_scaled_transpose, nn, n, b.T1, b.gif, b.Gi);
       syrk(s, false, n, n, 1.0, b.G, n, 0.0, b.W, n);
       LAUNCH(s, k_lower_to_full, nn, n, b.W);
+      CU(s, cudaMemcpyAsync(b.Gs, b.G, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s->st));
+      LAUNCH(s, k_div_cols, nn, n, b.Gs, b.sc);
+      syrk(s, false, n, n, 1.0, b.Gs, n, 0.0, b.Si, n);
+      LAUNCH(s, k_lower_to_full, nn, n, b.Si);
+      CU(s, cudaMemcpyAsync(b.Hx, b.Gi, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s->st));
+      LAUNCH(s, k_div_rows, nn, n, b.Hx, b.sc);
     }
   }
   if (s->ns) LAUNCH(s, k_inv, s->ns, s->ns, s->z, s->zinv);
@@ -924,8 +1005,9 @@ constexpr int kMaxRefine = 10;
 
 // dy = (H + reg I)^-1 h.  FP64: two triangular solves with the factor.
 // Mixed: the FP32-class factor's solution refined with FP64 residuals
-// h - (H + reg I) dy of the matrix-free operator until the residual stops
-// shrinking; if it then exceeds 1e-11 |h|, the Schur matrix is assembled
+// h - (H + reg I) dy of the matrix-free operator until the residual is
+// below 1e-12 |h| or stops halving; if it then exceeds 1e-11 |h|, the Schur
+// matrix is assembled
 // and factored in FP64 for this and every later iteration.
 bool solve_schur(S* s, bool* ok) {
   const int m = s->m;
@@ -946,7 +1028,7 @@ bool solve_schur(S* s, bool* ok) {
     const int rs = reduce(s, RED_MAXABS, m, s->ir_r);
     if (!fetch(s)) return false;
     rn = s->hslots[rs];
-    if (!(rn <= 1e-14 * hn) && rn < 0.5 * prev) {
+    if (!(rn <= 1e-12 * hn) && rn < 0.5 * prev) {
       prev = rn;
       chol_solve(s, s->ir_r, s->ir_d);
       LAUNCH(s, k_lin, m, m, s->dy, 1.0, s->dy, 1.0, s->ir_d, 0.0, nullptr, 0.0, nullptr, 0.0, nullptr);
@@ -1038,13 +1120,15 @@ void correction(S* s) {
 }
 
 // ---- Lanczos for lambda_min of a formed symmetric Z (blocks above
-// kLanczosMin; smaller blocks use the dense eigensolver).  Full
-// reorthogonalization; stops when the Ritz residual |beta_k s_k| of the
-// smallest Ritz value is below 1e-12 ||Z|| (eigenvalue error at most that),
-// at k = n, or gives up at kLanczosMax (the caller then uses the dense
+// kLanczosWarpMax).  Full reorthogonalization (twice); the step's scalars
+// stay on the device and the host reads them every kLanczosBatch steps to
+// apply the stopping rule at each step in order: the smallest Ritz value of
+// the first step whose Ritz residual |beta_k s_k| is below 1e-12 ||Z||, or
+// of step n.  Gives up at kLanczosMax (the caller then uses the dense
 // eigensolver).
-constexpr int kLanczosMin = 257;
+constexpr int kLanczosMin = 129;
 constexpr int kLanczosMax = 320;
+constexpr int kLanczosBatch = 8;
 constexpr int kLanczosWarpMax = 128;  // batched one-warp device Lanczos up to this size
 
 bool lanczos_eigmin(S* s, int n, const double* Z, double* out) {
@@ -1062,38 +1146,40 @@ bool lanczos_eigmin(S* s, int n, const double* Z, double* out) {
   for (auto& v : q0) v /= nrm;
   CU(s, cudaMemcpyAsync(Q, q0.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s->st));
   std::vector<double> al, be;
-  const double one = 1.0, zero = 0.0, mone = -1.0;
-  double beta_prev = 0.0;
+  std::vector<int> aslot, bslot;
   const int kmax = std::min(n, kLanczosMax);
-  for (int k = 0; k < kmax; ++k) {
-    const double* q = Q + (int64_t)k * n;
-    double* w = Q + (int64_t)(k + 1) * n;
-    CB(s, cublasDsymv(s->cb, CUBLAS_FILL_MODE_LOWER, n, &one, Z, n, q, 1, &zero, w, 1));
-    double alpha = 0.0;
-    CB(s, cublasDdot(s->cb, n, q, 1, w, 1, &alpha));
-    const double ma = -alpha;
-    CB(s, cublasDaxpy(s->cb, n, &ma, q, 1, w, 1));
-    if (k > 0) {
-      const double mb = -beta_prev;
-      CB(s, cublasDaxpy(s->cb, n, &mb, Q + (int64_t)(k - 1) * n, 1, w, 1));
+  const int ga = std::min(n, 152 * 16);
+  for (int k0 = 0; k0 < kmax; k0 += kLanczosBatch) {
+    const int k1 = std::min(kmax, k0 + kLanczosBatch);
+    for (int k = k0; k < k1; ++k) {
+      const double* q = Q + (int64_t)k * n;
+      double* w = Q + (int64_t)(k + 1) * n;
+      k_gemv_t<<<ga, kThreads, 0, s->st>>>(n, n, Z, n, q, w, 0);  // Z symmetric: Z'q = Zq
+      s->launches += 1;
+      const int sa = reduce(s, RED_DOT, n, q, w);
+      aslot.push_back(sa);
+      LAUNCH(s, k_lanczos_update, n, (int64_t)n, w, q, k ? Q + (int64_t)(k - 1) * n : nullptr, s->slots + sa,
+             k ? s->slots + bslot.back() : s->slots + sa);
+      for (int r = 0; r < 2; ++r) {
+        k_gemv_t<<<std::min(k + 1, 152 * 16), kThreads, 0, s->st>>>(n, k + 1, Q, n, w, s->lh, 0);
+        s->launches += 1;
+        LAUNCH(s, k_gemv_sub, n, (int64_t)n, k + 1, Q, (int64_t)n, s->lh, w);
+      }
+      const int sb = reduce(s, RED_DOT, n, w, w);
+      bslot.push_back(sb);
+      LAUNCH(s, k_normalize, n, (int64_t)n, w, s->slots + sb, w);
     }
-    for (int r = 0; r < 2; ++r) {
-      CB(s, cublasDgemv(s->cb, CUBLAS_OP_T, n, k + 1, &one, Q, n, w, 1, &zero, s->lh, 1));
-      CB(s, cublasDgemv(s->cb, CUBLAS_OP_N, n, k + 1, &mone, Q, n, s->lh, 1, &one, w, 1));
+    if (!fetch(s)) return false;
+    for (int k = k0; k < k1; ++k) {
+      al.push_back(s->hslots[aslot[k]]);
+      const double beta = std::sqrt(std::max(s->hslots[bslot[k]], 0.0));
+      double znorm = 0.0;
+      const double theta = tridiag_min(al, be, k + 1, &znorm);
+      if (k + 1 == n || beta <= 1e-300) { *out = theta; return true; }
+      const double resid = beta * tridiag_last_component(al, be, k + 1, theta, znorm);
+      if (resid <= 1e-12 * std::max(znorm, 1e-300)) { *out = theta; return true; }
+      be.push_back(beta);
     }
-    double beta = 0.0;
-    CB(s, cublasDnrm2(s->cb, n, w, 1, &beta));
-    if (s->fail) return false;
-    al.push_back(alpha);
-    double znorm = 0.0;
-    const double theta = tridiag_min(al, be, k + 1, &znorm);
-    if (k + 1 == n || beta <= 1e-300) { *out = theta; return true; }
-    const double resid = beta * tridiag_last_component(al, be, k + 1, theta, znorm);
-    if (resid <= 1e-12 * std::max(znorm, 1e-300)) { *out = theta; return true; }
-    be.push_back(beta);
-    const double inv = 1.0 / beta;
-    CB(s, cublasDscal(s->cb, n, &inv, w, 1));
-    beta_prev = beta;
   }
   return false;
 }
@@ -1172,9 +1258,19 @@ bool step_lengths(S* s, double* a_out, double* b_out) {
   int64_t qoff = 0, woff = 0;
   for (auto& b : s->B) {
     const int n = b.n;
-    // Z_X = Lx^-1 dX Lx^-T in T1, Z_S = Ls^-1 dS Ls^-T in T2
-    form_congruence(s, n, b.Lx, b.dX, b.T1);
-    form_congruence(s, n, b.Ls, b.dS, b.T2);
+    // Z_X ~ Lx^-1 dX Lx^-T in T1, Z_S ~ Ls^-1 dS Ls^-T in T2: NT by the
+    // orthogonally similar Hx dX Hx' and Gs' dS Gs (products only)
+    if (is_nt(s)) {
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.Hx, n, b.dX, n, 0.0, b.T3, n);
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_T, n, n, n, 1.0, b.T3, n, b.Hx, n, 0.0, b.T1, n);
+      LAUNCH(s, k_sym, (int64_t)n * n, n, b.T1);
+      gemm(s, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, 1.0, b.Gs, n, b.dS, n, 0.0, b.T3, n);
+      gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.T3, n, b.Gs, n, 0.0, b.T2, n);
+      LAUNCH(s, k_sym, (int64_t)n * n, n, b.T2);
+    } else {
+      form_congruence(s, n, b.Lx, b.dX, b.T1);
+      form_congruence(s, n, b.Ls, b.dS, b.T2);
+    }
     if (n <= kLanczosWarpMax) {
       for (int side = 0; side < 2; ++side) {
         const int slot = s->nslot++;
@@ -1594,6 +1690,15 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   s->H = vec((int64_t)m * m); s->H0 = vec((int64_t)m * m);
   s->ir_r = vec(m); s->ir_d = vec(m); s->ir_h = vec(m);
   if (dense_ws) { s->Tb = vec(dense_ws); s->Bb = vec(dense_ws); }
+  {
+    int64_t nn_dense = 0;
+    for (auto& b : s->B)
+      if (b.dense) nn_dense = std::max<int64_t>(nn_dense, (int64_t)b.n * b.n);
+    if (nn_dense) {
+      s->gpart = vec(nn_dense * kGemvChunks);
+      if (!s->gpart) return bail(MSDP_ERR_OUT_OF_MEMORY);
+    }
+  }
   s->partial = vec(kRedBlocks); s->slots = vec(kSlots);
   s->dinfo = dalloc<int>(s, kInfos);
   bool okalloc = s->b && s->dlin && s->Clin && s->Cw && s->y && s->dy && s->Rp && s->h && s->acc && s->x && s->z &&
@@ -1610,13 +1715,13 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
     const int n = b.n;
     const int64_t nn = (int64_t)n * n;
     double** mats[] = {&b.C, &b.X, &b.S, &b.Rd, &b.Ls, &b.Si, &b.Lx, &b.W, &b.G, &b.Gi,
-                       &b.dX, &b.dS, &b.corr, &b.ERd, &b.T1, &b.T2, &b.T3};
+                       &b.dX, &b.dS, &b.corr, &b.ERd, &b.T1, &b.T2, &b.T3, &b.Gs, &b.Hx};
     for (double** p : mats) {
       *p = vec(nn);
       if (!*p) return bail(MSDP_ERR_OUT_OF_MEMORY);
     }
-    b.lam = vec(n); b.D = vec(n); b.sc = vec(n); b.w = vec(n);
-    if (!b.lam || !b.D || !b.sc || !b.w) return bail(MSDP_ERR_OUT_OF_MEMORY);
+    b.lam = vec(n); b.D = vec(n); b.sc = vec(n); b.w = vec(n); b.gif = vec(n);
+    if (!b.lam || !b.D || !b.sc || !b.w || !b.gif) return bail(MSDP_ERR_OUT_OF_MEMORY);
     int lw = 0;
     cusolverDnDpotrf_bufferSize(s->cs, CUBLAS_FILL_MODE_LOWER, n, b.X, n, &lw); lwork = std::max(lwork, lw);
     cusolverDnDpotri_bufferSize(s->cs, CUBLAS_FILL_MODE_LOWER, n, b.X, n, &lw); lwork = std::max(lwork, lw);
@@ -1692,7 +1797,7 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   int nmax = 0;
   for (auto& b : s->B) nmax = std::max(nmax, b.n);
   if (nmax >= kLanczosMin) {
-    s->lq = vec((int64_t)nmax * (kLanczosMax + 1));
+    s->lq = vec((int64_t)nmax * (std::min(nmax, kLanczosMax) + 1));
     s->lh = vec(kLanczosMax + 1);
     if (!s->lq || !s->lh) return bail(MSDP_ERR_OUT_OF_MEMORY);
   }

@@ -119,11 +119,13 @@ def test_tc_gemm_rejects_bad_arguments(gpu_ctx):
     assert lib.msdp_tc_gemm(0, 0, 0, 0, 0, 4, 1.0, null, 4, null, 4, 0.0, null, 1, 0, null) == 0
 
 
-@pytest.mark.parametrize("prec,tol", [(0, 2e-14), (1, 1e-6)])
+@pytest.mark.parametrize("prec,tol", [(0, 5e-14), (1, 1e-6)])
 def test_tc_gemm_config3_schur_shape(gpu_ctx, prec, tol):
     """The Schur-complement product of the dense-constraint workload at full
     size: H = B B' (lower) with B of 2000 rows and K = 20100 (the symmetric
-    vectors of the 200 x 200 block), against a float64 product on the GPU."""
+    vectors of the 200 x 200 block), against a float64 product on the GPU.
+    At this K the float64 reference itself is off by about sqrt(K) * 2^-53
+    = 1.6e-14 of |B||B'|, hence the bound."""
     import torch
 
     from madsdp_gpu import _lib
