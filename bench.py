@@ -32,9 +32,14 @@ for _p in (ROOT, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-# request mix of the served stream (Poisson arrivals); sizes are those one
-# CTA per request solves at interactive latency
-SERVE_MIX = {"sos_d": (5, 127), "maxcut_n": (20, 100), "dense_n": (8, 32), "dense_m": 200}
+# request mixes of the served stream (Poisson arrivals): the serving
+# workload's stated mix (max-cut n up to 800 and dense requests with m up to
+# 3000 run in the server's whole-GPU slots), and a compact mix that one
+# thread block per request serves
+SERVE_MIXES = {
+    "stated": {"sos_d": (5, 127), "maxcut_n": (50, 800), "dense_n": (32, 256), "dense_m": 3000, "dense_m_min": 100},
+    "compact": {"sos_d": (5, 127), "maxcut_n": (20, 100), "dense_n": (8, 32), "dense_m": 200, "dense_m_min": 10},
+}
 
 METRIC = "SDP solves/sec + p50/p99 latency at 1e-7 gap: mixed/batched vs FP64 GPU vs CPU"
 UNIT = "solves/s"
@@ -708,21 +713,29 @@ def run_gpu(args):
     serving = None
     if args.serve_seconds > 0:
         from madsdp_gpu.serving import Server, poisson_stream, serve_stream
-        stream = poisson_stream(args.serve_rate, args.serve_seconds, seed=args.seed + 17 + rank,
-                                sos_d=SERVE_MIX["sos_d"], maxcut_n=SERVE_MIX["maxcut_n"],
-                                dense_n=SERVE_MIX["dense_n"], dense_m=SERVE_MIX["dense_m"])
-        srv = Server(memory_budget_bytes=8 << 30, max_slots=4096, precision="mixed", context=ctx)
-        serving = serve_stream(srv, stream, iterations=args.serve_iterations, time_limit=600.0,
+        mix = SERVE_MIXES[args.serve_mix]
+        stream = poisson_stream(args.serve_rate, args.serve_seconds, seed=args.seed + 17 + rank, **mix)
+        srv = Server(memory_budget_bytes=8 << 30, max_slots=4096, precision="mixed", context=ctx,
+                     whole_gpu_slots=args.serve_whole_gpu_slots, whole_gpu_memory_bytes=64 << 30)
+        serving = serve_stream(srv, stream, iterations=args.serve_iterations, time_limit=1800.0,
                                budget_s=args.serve_budget_ms / 1e3)
         srv.close()
         serving.update({"rate_per_s": args.serve_rate, "duration_s": args.serve_seconds,
                         "iterations_per_wave": args.serve_iterations, "wave_budget_ms": args.serve_budget_ms,
-                        "memory_budget_bytes": 8 << 30,
-                        "mix": "50%% SOS d~U%s, 30%% max-cut n~U%s p=4/n, 20%% dense one block n~U%s m<=min(%d, n(n+1)/2)"
-                               % (SERVE_MIX["sos_d"], SERVE_MIX["maxcut_n"], SERVE_MIX["dense_n"], SERVE_MIX["dense_m"]),
+                        "memory_budget_bytes": 8 << 30, "whole_gpu_slots": args.serve_whole_gpu_slots,
+                        "whole_gpu_memory_bytes": 64 << 30, "mix_name": args.serve_mix,
+                        "mix": "50%% SOS d~U%s, 30%% max-cut n~U%s p=4/n, 20%% dense one block n~U%s "
+                               "m~U(%d, %d) capped at n(n+1)/2; requests with a block above 64 or m above 300 run "
+                               "in whole-GPU slots" % (mix["sos_d"], mix["maxcut_n"], mix["dense_n"],
+                                                      mix["dense_m_min"], mix["dense_m"]),
                         "latency": "host clock, arrival to result available"})
         if rank == 0 and world == 1 and not args.no_cpu:
-            serving["cpu_replay"] = cpu_serve_replay(stream, os.cpu_count() or 1, args.cpu_seconds)
+            if args.serve_mix == "compact":
+                serving["cpu_replay"] = cpu_serve_replay(stream, os.cpu_count() or 1, args.cpu_seconds)
+            else:
+                serving["cpu_replay"] = {"note": "not run for this mix: the compiled restatement (no BLAS) needs "
+                                                 "minutes per dense request with m in the thousands, so a bounded "
+                                                 "sample would not finish its solves in flight"}
 
     if rank != 0:
         return
@@ -795,6 +808,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-mix", default="stated", choices=sorted(SERVE_MIXES))
+    ap.add_argument("--serve-whole-gpu-slots", type=int, default=4)
     ap.add_argument("--serve-iterations", type=int, default=1000)
     ap.add_argument("--serve-budget-ms", type=float, default=20.0)
     ap.add_argument("--workload", default="sos_batch", choices=["sos_batch", *INSTANCE_WORKLOADS])

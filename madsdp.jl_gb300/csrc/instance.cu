@@ -220,13 +220,23 @@ __global__ void k_lanczos_update(int64_t n, double* __restrict__ w, const double
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     w[i] -= a * q[i] + (p ? b * p[i] : 0.0);
 }
-// out[i] -= sum_j A[i + j lda] v[j]
-__global__ void k_gemv_sub(int64_t rows, int cols, const double* __restrict__ A, int64_t lda,
-                           const double* __restrict__ v, double* __restrict__ out) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int j = 0; j < cols; ++j) s = fma(A[i + j * lda], v[j], s);
-    out[i] -= s;
+// out[i] -= sum_j A[i + j lda] v[j]: 32 rows per block of 32 x 32 threads,
+// thread (r, g) sums columns g, g + 32, ... (coalesced over r); the 32
+// partial sums of a row are added in a fixed order
+__global__ void __launch_bounds__(1024) k_gemv_sub(int64_t rows, int cols, const double* __restrict__ A, int64_t lda,
+                                                  const double* __restrict__ v, double* __restrict__ out) {
+  __shared__ double part[32][33];
+  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int64_t i = (int64_t)blockIdx.x * 32 + r;
+  double s = 0.0;
+  if (i < rows)
+    for (int j = g; j < cols; j += 32) s = fma(A[i + j * lda], v[j], s);
+  part[g][r] = s;
+  __syncthreads();
+  if (g == 0 && i < rows) {
+    double t = 0.0;
+    for (int q = 0; q < 32; ++q) t += part[q][r];
+    out[i] -= t;
   }
 }
 // out = w / sqrt(*pbb)
@@ -1163,7 +1173,8 @@ bool lanczos_eigmin(S* s, int n, const double* Z, double* out) {
       for (int r = 0; r < 2; ++r) {
         k_gemv_t<<<std::min(k + 1, 152 * 16), kThreads, 0, s->st>>>(n, k + 1, Q, n, w, s->lh, 0);
         s->launches += 1;
-        LAUNCH(s, k_gemv_sub, n, (int64_t)n, k + 1, Q, (int64_t)n, s->lh, w);
+        k_gemv_sub<<<(n + 31) / 32, 1024, 0, s->st>>>((int64_t)n, k + 1, Q, (int64_t)n, s->lh, w);
+        s->launches += 1;
       }
       const int sb = reduce(s, RED_DOT, n, w, w);
       bslot.push_back(sb);

@@ -10,7 +10,9 @@ serving workload (SOS, max-cut and dense SDPs) from a seed.
 from __future__ import annotations
 
 import ctypes as C
+import threading
 import time
+from collections import deque
 from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
@@ -18,17 +20,130 @@ import numpy as np
 from . import _lib, generators as g
 from .components import DenseCholesky, EigenStep, Mehrotra, NT, Options, PrimalDual, ScaledIdentity, Status
 from .model import Model
-from .solver import Context, _Marshalled, _components, _options, _ptr, _stats_dict, default_context
+from .solver import (Context, InstanceSolver, _Marshalled, _components, _options, _ptr, _stats_dict,
+                     _use_instance_engine, default_context)
 
-__all__ = ["Server", "poisson_stream", "serve_stream"]
+__all__ = ["Server", "poisson_stream", "serve_stream", "instance_bytes_estimate"]
+
+LARGE_ID0 = 1 << 40  # request ids of whole-GPU requests start here
+
+
+def instance_bytes_estimate(model: Model) -> int:
+    """Device bytes of the whole-GPU solver for `model` (its allocations at
+    creation: block matrices, tensor-core operand slices, Schur matrices,
+    and for dense constraint blocks the constraint data, its slices and the
+    assembly's operands)."""
+    m = model.m
+    nmax = max(model.sides, default=1)
+    b = 8 * (19 * sum(n * n for n in model.sides) + 2 * m * m + max(nmax * nmax, m * m) + 8 * m)
+    b += 28 * (nmax + 128) * (nmax + 32)
+    if nmax > 128:
+        b += 8 * nmax * (min(nmax, 320) + 1)
+    for n, A in zip(model.sides, model.A):
+        if A.nnz >= m * n * n // 2:
+            b += (24 + 14 + 14 + 7) * m * n * n + 128 * n * n
+    return int(b)
+
+
+class _WholeGPURequests:
+    """Requests too large for one thread block, each solved on the whole GPU
+    (InstanceSolver) by one of `slots` worker threads.  Every worker owns a
+    context (its own stream), so these solves overlap on the device with
+    each other and with the batched waves; they are started in arrival order
+    while the estimated device bytes of the running solves fit
+    `memory_budget_bytes` (one runs regardless when none is running)."""
+
+    def __init__(self, slots: int, memory_budget_bytes: int, device: int, kwargs: dict):
+        self.kwargs = kwargs
+        self.budget = int(memory_budget_bytes)
+        self.cv = threading.Condition()
+        self.queue = deque()           # (rid, model, estimate)
+        self.running: Dict[int, int] = {}
+        self.results: Dict[int, dict] = {}
+        self.done: List[int] = []
+        self.used = 0
+        self.stop = False
+        self.error: Optional[BaseException] = None
+        self.threads = [threading.Thread(target=self._work, args=(device,), daemon=True) for _ in range(slots)]
+        for t in self.threads:
+            t.start()
+
+    def submit(self, rid: int, model: Model):
+        with self.cv:
+            self.queue.append((rid, model, instance_bytes_estimate(model)))
+            self.cv.notify_all()
+
+    def _next(self):
+        # called with the lock held: the head of the queue when it fits
+        if self.queue and (not self.running or self.used + self.queue[0][2] <= self.budget):
+            rid, model, est = self.queue.popleft()
+            self.running[rid] = est
+            self.used += est
+            return rid, model
+        return None
+
+    def _work(self, device: int):
+        ctx = Context(device)
+        while True:
+            with self.cv:
+                job = None
+                while not self.stop and job is None:
+                    job = self._next()
+                    if job is None:
+                        self.cv.wait(0.05)
+                if self.stop:
+                    return
+            rid, model = job
+            try:
+                s = InstanceSolver(model, context=ctx, **self.kwargs)
+                s.solve()
+                st = s.stats()
+                X, y, x, z = s.solution()
+                s.close()
+                res = dict(st)
+                res.update(X=X, y=y, x=x, z=z, finish=time.perf_counter())
+            except BaseException as e:  # surfaced by the owning server
+                res = None
+                with self.cv:
+                    self.error = e
+            with self.cv:
+                self.used -= self.running.pop(rid)
+                if res is not None:
+                    self.results[rid] = res
+                    self.done.append(rid)
+                self.cv.notify_all()
+
+    def counts(self) -> Tuple[int, int]:
+        with self.cv:
+            if self.error is not None:
+                raise RuntimeError(f"whole-GPU request failed: {self.error!r}")
+            return len(self.queue), len(self.running)
+
+    def finished(self) -> List[int]:
+        with self.cv:
+            out, self.done = self.done, []
+            return out
+
+    def close(self):
+        with self.cv:
+            self.stop = True
+            self.cv.notify_all()
+        for t in self.threads:
+            t.join()
 
 
 class Server:
-    """A continuous-batching solve server on one GPU (msdp_server)."""
+    """A continuous-batching solve server on one GPU (msdp_server).
+
+    `whole_gpu_slots` > 0 adds a slot type for requests that the solver
+    would run on the whole GPU (a block above 64 or more than 300
+    constraints): they are solved by that many concurrent whole-GPU solvers,
+    admitted by `whole_gpu_memory_bytes`, beside the batched waves."""
 
     def __init__(self, memory_budget_bytes: int = 1 << 30, max_slots: int = 1024, direction=None,
                  step=None, centering=None, initial_point=None, schur=None, precision: str = "fp64",
-                 context: Optional[Context] = None, **options):
+                 context: Optional[Context] = None, whole_gpu_slots: int = 0,
+                 whole_gpu_memory_bytes: int = 16 << 30, **options):
         self.ctx = context or default_context()
         self.lib = self.ctx.lib
         alg = PrimalDual(direction or NT(), step or EigenStep(), centering or Mehrotra())
@@ -42,9 +157,19 @@ class Server:
             raise RuntimeError(f"msdp_server_create failed: {_lib.ERRORS.get(rc, rc)}")
         self.h = h
         self.models: Dict[int, Model] = {}
+        self.large = None
+        self._next_large = LARGE_ID0
+        if whole_gpu_slots > 0:
+            kw = dict(direction=alg.direction, step=alg.step, centering=alg.centering,
+                      initial_point=initial_point or ScaledIdentity(), schur=schur or DenseCholesky(),
+                      precision=precision, **options)
+            self.large = _WholeGPURequests(whole_gpu_slots, whole_gpu_memory_bytes, self.ctx.device, kw)
         self.ctx.adopt(self)
 
     def close(self):
+        if getattr(self, "large", None) is not None:
+            self.large.close()
+            self.large = None
         if getattr(self, "h", None):
             self.lib.msdp_server_destroy(self.h)
             self.h = None
@@ -56,6 +181,12 @@ class Server:
             pass
 
     def submit(self, model: Model) -> int:
+        if self.large is not None and _use_instance_engine(model):
+            rid = self._next_large
+            self._next_large += 1
+            self.models[rid] = model
+            self.large.submit(rid, model)
+            return rid
         mm = _Marshalled(model)
         rid = C.c_int64()
         rc = self.lib.msdp_server_submit(self.h, C.byref(mm.desc), C.byref(rid))
@@ -71,6 +202,11 @@ class Server:
         stream without waiting (waves overlap on the GPU); each request of
         a wave runs until the wave has lasted budget_s and every request
         of it has iterated once."""
+        if self.large is not None:
+            p, a, _ = self._batched_counts()
+            if p == 0 and a == 0:
+                time.sleep(5e-4)  # only whole-GPU requests are running (in their threads)
+                return 0, 0
         act, done = C.c_int32(), C.c_int32()
         if budget_s > 0:
             rc = self.lib.msdp_server_step_budget(self.h, int(iterations), float(budget_s), C.byref(act),
@@ -81,10 +217,19 @@ class Server:
             raise RuntimeError(f"msdp_server_step: {_lib.ERRORS.get(rc, rc)}")
         return act.value, done.value
 
-    def counts(self) -> Tuple[int, int, int]:
+    def _batched_counts(self) -> Tuple[int, int, int]:
         p, a, c = C.c_int32(), C.c_int32(), C.c_int64()
         self.lib.msdp_server_counts(self.h, C.byref(p), C.byref(a), C.byref(c))
         return p.value, a.value, c.value
+
+    def counts(self) -> Tuple[int, int, int]:
+        """(pending, active, completed) over both slot types."""
+        p, a, c = self._batched_counts()
+        if self.large is not None:
+            lp, la = self.large.counts()
+            p, a = p + lp, a + la
+            c += len(self.large.results)
+        return p, a, c
 
     @property
     def launch_count(self) -> int:
@@ -92,6 +237,13 @@ class Server:
 
     def result(self, rid: int) -> Optional[dict]:
         """The finished request's stats and solution, or None if still running."""
+        if rid >= LARGE_ID0:
+            with self.large.cv:
+                r = self.large.results.pop(rid, None)
+            if r is None:
+                return None
+            del self.models[rid]
+            return r
         model = self.models[rid]
         X = [np.zeros((n, n), order="F") for n in model.sides]
         Xp = (C.POINTER(C.c_double) * max(len(X), 1))(*[_ptr(a) for a in X])
@@ -110,7 +262,7 @@ class Server:
 
     def finished(self, capacity: int = 4096) -> List[int]:
         """Ids of requests finished since the last call, each reported once."""
-        out: List[int] = []
+        out: List[int] = [] if self.large is None else self.large.finished()
         buf = (C.c_int64 * capacity)()
         cnt = C.c_int32()
         while True:
@@ -134,20 +286,21 @@ class Server:
         raise RuntimeError("server did not drain")
 
 
-def _dense_request(rng, nmin: int, nmax: int, mmax: int, seed: int) -> Model:
+def _dense_request(rng, nmin: int, nmax: int, mmax: int, seed: int, mmin: int = 10) -> Model:
     n = int(rng.integers(nmin, nmax + 1))
-    m = int(rng.integers(min(10, n * (n + 1) // 2), min(mmax, n * (n + 1) // 2) + 1))
+    cap = n * (n + 1) // 2
+    m = int(rng.integers(min(mmin, cap), min(mmax, cap) + 1))
     return g.dense_random([n], 0, m, seed=seed)
 
 
 def poisson_stream(rate: float, duration: float, seed: int = 0, sos_d=(5, 63), maxcut_n=(20, 64),
-                   dense_n=(8, 24), dense_m=60) -> List[Tuple[float, str, Model]]:
+                   dense_n=(8, 24), dense_m=60, dense_m_min: int = 10) -> List[Tuple[float, str, Model]]:
     """(arrival time, kind, model) for Poisson arrivals at `rate` per second.
 
     The mix is 50% SOS lower bounds (Gram side d+1, d ~ U(sos_d)), 30% max-cut
     (n ~ U(maxcut_n), edge probability 4/n) and 20% random dense SDPs (one
-    block n ~ U(dense_n), m <= min(dense_m, n(n+1)/2), no scalars; m is capped
-    because larger m makes the constraint map rank-deficient).
+    block n ~ U(dense_n), m ~ U(dense_m_min, dense_m) capped at n(n+1)/2, no
+    scalars; the cap keeps the constraint map of full rank).
     """
     rng = np.random.default_rng(seed)
     t, out, k = 0.0, [], 0
@@ -163,7 +316,7 @@ def poisson_stream(rate: float, duration: float, seed: int = 0, sos_d=(5, 63), m
             n = int(rng.integers(maxcut_n[0], maxcut_n[1] + 1))
             out.append((t, "maxcut", g.maxcut(n, min(1.0, 4.0 / n), seed=s)))
         else:
-            out.append((t, "dense", _dense_request(rng, dense_n[0], dense_n[1], dense_m, s)))
+            out.append((t, "dense", _dense_request(rng, dense_n[0], dense_n[1], dense_m, s, dense_m_min)))
         k += 1
     return out
 

@@ -201,7 +201,7 @@ def test_sos_batch_mixed(gpu_ctx):
         assert st["status"] == M.Status.SOLVE_SUCCEEDED, (i, st)
         assert max(st["inf_pr"], st["inf_du"], st["gap"]) <= 1e-7
         scale = max(1.0, abs(ref.primal_objective()) + abs(ref.dual_objective()))
-        assert abs(st["pobj"] - ref.primal_objective()) <= 5e-7 * scale
+        assert abs(st["pobj"] - ref.primal_objective()) <= 1e-7 * scale
         assert st["iter_fp32"] >= 1
 
 
@@ -232,7 +232,7 @@ def test_mixed_blocks_beyond_shared_memory(gpu_ctx):
         assert st["status"] == M.Status.SOLVE_SUCCEEDED, st
         assert max(st["inf_pr"], st["inf_du"], st["gap"]) <= 1e-7
         scale = max(1.0, abs(ref.primal_objective()) + abs(ref.dual_objective()))
-        assert abs(st["pobj"] - ref.primal_objective()) <= 5e-7 * scale
+        assert abs(st["pobj"] - ref.primal_objective()) <= 1e-7 * scale
 
 
 def test_batch_uneven_results_independent_of_mix(gpu_ctx):
@@ -263,7 +263,7 @@ def test_dense_constraints_column_assembly(gpu_ctx, direction, precision):
         ref = o.Solver(m, direction=getattr(o, direction)()).solve()
         assert st["status"] == M.Status.SOLVE_SUCCEEDED, st
         scale = max(1.0, abs(ref.primal_objective()) + abs(ref.dual_objective()))
-        assert abs(st["pobj"] - ref.primal_objective()) <= (1e-7 if precision == "fp64" else 5e-7) * scale
+        assert abs(st["pobj"] - ref.primal_objective()) <= 1e-7 * scale
         if precision == "fp64":
             assert abs(st["iter"] - ref.iter) <= 1
 

@@ -120,9 +120,9 @@ def test_serve_poisson_stream(gpu_ctx):
     assert out["p99_latency_ms"] >= out["p50_latency_ms"] > 0
 
 
-@pytest.mark.parametrize("precision,rtol", [("fp64", 1e-7), ("mixed", 5e-7)])
+@pytest.mark.parametrize("precision,rtol", [("fp64", 1e-7), ("mixed", 1e-7)])
 def test_served_mix_matches_oracle(gpu_ctx, precision, rtol):
-    """Every request of a served Poisson stream with the benchmark's mix
+    """Every request of a served Poisson stream with the compact mix
     (SOS d <= 127, max-cut n <= 100, dense n <= 32 with m <= 200) converges
     and agrees with the compiled oracle: objectives within
     rtol * max(1, |p| + |d|) (the FP64 and mixed tolerances of the batch
@@ -131,7 +131,7 @@ def test_served_mix_matches_oracle(gpu_ctx, precision, rtol):
 
     import bench
     from oracle import cpu_ipm
-    stream = poisson_stream(40.0, 1.5, seed=23, **bench.SERVE_MIX)
+    stream = poisson_stream(40.0, 1.5, seed=23, **bench.SERVE_MIXES["compact"])
     models = [m for _, _, m in stream]
     ref = cpu_ipm.solve_many(models, threads=os.cpu_count() or 1)
     srv = Server(memory_budget_bytes=2 << 30, max_slots=256, precision=precision)
@@ -144,4 +144,73 @@ def test_served_mix_matches_oracle(gpu_ctx, precision, rtol):
         assert s["status"] == M.Status.SOLVE_SUCCEEDED, (rid, kind, s["status"])
         scale = max(1.0, abs(r["pobj"]) + abs(r["dobj"]))
         assert abs(s["pobj"] - r["pobj"]) <= rtol * scale, (rid, kind, s["pobj"], r["pobj"])
+    srv.close()
+
+
+def test_whole_gpu_requests_same_alone_and_in_the_mix(gpu_ctx):
+    """Requests above one thread block (a max-cut with n = 300, a dense
+    block of 120 with m = 600) are served by the whole-GPU slot type while
+    small ones run in batched waves, all at once and overlapping on the GPU;
+    every result equals solving the request alone (small: a one-problem
+    batch; large: the whole-GPU solver)."""
+    small = mixed_requests()[:4]
+    large = [g.maxcut(300, 4.0 / 300, seed=21), g.dense_random([120], 0, 600, seed=22)]
+    srv = Server(memory_budget_bytes=64 << 20, max_slots=16, whole_gpu_slots=2)
+    ids = [srv.submit(m) for m in small[:2]] + [srv.submit(m) for m in large] + [srv.submit(m) for m in small[2:]]
+    models = small[:2] + large + small[2:]
+    srv.drain(3, budget_s=0.002)
+    assert srv.counts()[:2] == (0, 0)
+    assert sorted(srv.finished()) == sorted(ids)
+    for rid, m in zip(ids, models):
+        r = srv.result(rid)
+        assert r is not None
+        if m in large:
+            s = M.InstanceSolver(m).solve()
+            st = s.stats()
+            X, y, _, _ = s.solution()
+            s.close()
+        else:
+            st, X, y = alone(m)
+        assert st["status"] == M.Status.SOLVE_SUCCEEDED
+        assert_same(r, st, X, y)
+    srv.close()
+
+
+def test_served_stated_mix_subsample_matches_oracle(gpu_ctx):
+    """The serving workload's stated mix (SOS d <= 127, max-cut n in
+    [50, 800], dense n in [32, 256] with m in [100, 3000]) through the server
+    with whole-GPU slots for the large requests, in mixed precision: the
+    requests of a seeded stream that the compiled oracle solves in seconds
+    (max-cut n <= 400, dense m n^2 <= 2e7) are served together; each
+    converges and agrees with the oracle to 1e-7 * max(1, |p| + |d|)."""
+    import os
+
+    import bench
+    from madsdp_gpu.solver import _use_instance_engine
+    from oracle import cpu_ipm
+    stream = poisson_stream(200.0, 0.5, seed=29, **bench.SERVE_MIXES["stated"])
+
+    def cheap(kind, m):
+        if kind == "maxcut":
+            return m.sides[0] <= 400
+        if kind == "dense":
+            return m.m * m.sides[0] ** 2 <= 2e7
+        return True
+
+    keep = [(k, m) for _, k, m in stream if cheap(k, m)][:24]
+    kinds = [k for k, _ in keep]
+    models = [m for _, m in keep]
+    large = [_use_instance_engine(m) for m in models]
+    assert any(l and k == "maxcut" for k, l in zip(kinds, large))
+    assert any(l and k == "dense" for k, l in zip(kinds, large))
+    ref = cpu_ipm.solve_many(models, threads=os.cpu_count() or 1)
+    srv = Server(memory_budget_bytes=2 << 30, max_slots=256, precision="mixed", whole_gpu_slots=2)
+    ids = [srv.submit(m) for m in models]
+    srv.drain(50, budget_s=0.005)
+    for rid, kind, r in zip(ids, kinds, ref):
+        s = srv.result(rid)
+        assert r["status"] == 1
+        assert s["status"] == M.Status.SOLVE_SUCCEEDED, (rid, kind, s["status"])
+        scale = max(1.0, abs(r["pobj"]) + abs(r["dobj"]))
+        assert abs(s["pobj"] - r["pobj"]) <= 1e-7 * scale, (rid, kind, s["pobj"], r["pobj"])
     srv.close()
