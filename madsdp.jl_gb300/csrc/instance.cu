@@ -407,6 +407,48 @@ __global__ void k_gemv_t(int64_t rows, int cols, const double* __restrict__ A, i
   }
 }
 
+// ---- rank-one constraint blocks: A_j = sg_j v_j v_j' with V = [v_1 ... v_m]
+// H[j, k] += sg_j sg_k Q1[j, k] Q2[j, k] for j >= k (NT: Q1 = Q2 = V'WV;
+// HKM: Q1 = V'S^-1 V, Q2 = V'XV)
+__global__ void k_lowrank_schur(int m, const double* __restrict__ Q1, const double* __restrict__ Q2,
+                                const double* __restrict__ sg, double* __restrict__ H) {
+  const int64_t mm = (int64_t)m * m;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < mm; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(idx % m), k = (int)(idx / m);
+    if (j >= k) H[idx] += sg[j] * sg[k] * Q1[idx] * Q2[idx];
+  }
+}
+// out[j] (+)= sg_j sum_r V[r + j n] P[r + j n]  (one block per column)
+__global__ void k_lowrank_dots(int n, int m, const double* __restrict__ V, const double* __restrict__ P,
+                               const double* __restrict__ sg, double* __restrict__ out, int accumulate) {
+  __shared__ double red[kThreads / 32];
+  for (int j = blockIdx.x; j < m; j += gridDim.x) {
+    const double* v = V + (int64_t)j * n;
+    const double* q = P + (int64_t)j * n;
+    double s = 0.0;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) s = fma(v[r], q[r], s);
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+      t *= sg[j];
+      out[j] = accumulate ? out[j] + t : t;
+    }
+    __syncthreads();
+  }
+}
+// Vs[r + j n] = V[r + j n] sg_j y_j
+__global__ void k_lowrank_scale(int n, int m, const double* __restrict__ V, const double* __restrict__ sg,
+                                const double* __restrict__ y, double* __restrict__ Vs) {
+  const int64_t nm = (int64_t)n * m;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nm; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(idx / n);
+    Vs[idx] = V[idx] * sg[j] * y[j];
+  }
+}
+
 // H[j, k] += <A_j, L A_k R> for j >= k: sum over entry pairs
 // v_e v_f L[r_e, r_f] R[c_f, c_e] (the semantics of LowRankOpt's
 // schur_complement!, src/solver.jl:30-31,117-118).
@@ -447,6 +489,12 @@ struct Blk {
   int32_t *erow = nullptr, *ecol = nullptr, *pcon = nullptr;
   double *eval = nullptr, *pval = nullptr;
   double* Aall = nullptr;  // dense: n x (n m), column j*n.. of A_j
+  // rank-one constraints (every A_j = sg_j v_j v_j'): V (n x m), signs,
+  // V's columns sliced as rows (K = n) in both precisions, V's rows (K = m),
+  // and an n x m temporary
+  bool lowrank = false;
+  double *V = nullptr, *sg = nullptr, *P = nullptr;
+  tcg::Sliced vk[2], vr;
   // NT: Gs = G D^-1/2 and Hx = D^-1/2 Gi for S^-1 = Gs Gs' and the
   // step-length matrices Hx dX Hx', Gs' dS Gs (orthogonally similar to
   // Lx^-1 dX Lx^-T and Ls^-1 dS Ls^-T)
@@ -477,6 +525,9 @@ struct msdp_solver {
   double *corrlin = nullptr, *vlin = nullptr, *ctv = nullptr, *wlin = nullptr;
   double *H = nullptr, *H0 = nullptr, *Tb = nullptr, *Bb = nullptr;
   double* gpart = nullptr;  // partial sums of the dense A*(y) (kGemvChunks x n^2)
+  double *Q1 = nullptr, *Q2 = nullptr;  // m x m products of the rank-one assembly
+  tcg::Sliced tL;                        // operand slices of the rank-one products (n x m or m x n)
+  void* tLm = nullptr;
   // tensor-core products: operand slices of the n x n products (tA, tB),
   // the per-iteration operands of the dense assembly (tQ, tS), C_lin and
   // C_lin diag(x/z) (tCl, tCw), the fixed-point workspace and error flag
@@ -699,7 +750,16 @@ bool chol_ok(S* s, const CholCheck& c) { return s->hinfo[c.info] == 0 && s->hslo
 
 // ---- constraint operators of one block
 void jprod(S* s, Blk& b, const double* X, double* out, bool accumulate) {
-  if (b.dense) {
+  if (b.lowrank) {
+    // A(X)_j = sg_j v_j' X v_j: P = X V on the tensor cores, then column dots
+    const int n = b.n;
+    if (!tc_bind(s, &s->tA, s->tAm, n, n, 7)) return;
+    tc_slice(s, op_rows(X, n, true, n, n), &s->tA);
+    tc_product(s, s->tA, b.vk[0], tcg::kFp64, b.P, n, 1.0, 0.0, false);
+    k_lowrank_dots<<<std::min(s->m, 152 * 16), kThreads, 0, s->st>>>(n, s->m, b.V, b.P, b.sg, out,
+                                                                   accumulate ? 1 : 0);
+    s->launches += 1;
+  } else if (b.dense) {
     const int64_t nn = (int64_t)b.n * b.n;
     k_gemv_t<<<std::min(s->m, 152 * 16), kThreads, 0, s->st>>>(nn, s->m, b.Aall, nn, X, out, accumulate ? 1 : 0);
     s->launches += 1;
@@ -710,7 +770,14 @@ void jprod(S* s, Blk& b, const double* X, double* out, bool accumulate) {
 
 void jtprod(S* s, Blk& b, const double* yv, double* out) {
   const int64_t nn = (int64_t)b.n * b.n;
-  if (b.dense) {
+  if (b.lowrank) {
+    // A*(y) = V diag(sg y) V'
+    const int n = b.n, m = s->m;
+    LAUNCH(s, k_lowrank_scale, (int64_t)n * m, n, m, b.V, b.sg, yv, b.P);
+    if (!tc_bind(s, &s->tL, s->tLm, n, m, 7)) return;
+    tc_slice(s, op_rows(b.P, n, false, n, m), &s->tL);
+    tc_product(s, s->tL, b.vr, tcg::kFp64, out, n, 1.0, 0.0, false);
+  } else if (b.dense) {
     // A*(y) streams all of A: columns split over kGemvChunks block rows
     const dim3 grid((unsigned)std::min<int64_t>((nn + kThreads - 1) / kThreads, 152 * 8), kGemvChunks);
     k_gemv_n_part<<<grid, kThreads, 0, s->st>>>(nn, s->m, b.Aall, nn, yv, s->gpart);
@@ -899,7 +966,18 @@ void schur_complement(S* s, double* H, tcg::Mode mode) {
     const double* L = is_nt(s) ? b.W : b.Si;
     const double* R = is_nt(s) ? b.W : b.X;
     const int64_t mn = (int64_t)m * n;
-    if (!b.dense) {
+    if (b.lowrank) {
+      // NT: Q = V'WV, H += sg sg' o Q o Q; HKM: H += sg sg' o (V'S^-1 V) o (V'XV)
+      for (int side = 0; side < (is_nt(s) ? 1 : 2); ++side) {
+        const double* Lm = side ? R : L;
+        if (!tc_bind(s, &s->tA, s->tAm, n, n, nsl) || !tc_bind(s, &s->tL, s->tLm, m, n, nsl)) return;
+        tc_slice(s, op_rows(Lm, n, true, n, n), &s->tA);
+        tc_product(s, s->tA, b.vk[mi], mode, b.P, n, 1.0, 0.0, false);            // P = Lm V
+        tc_slice(s, op_rows(b.P, n, true, m, n), &s->tL);                        // rows: columns of P
+        tc_product(s, b.vk[mi], s->tL, mode, side ? s->Q2 : s->Q1, m, 1.0, 0.0, true);  // V' P (lower)
+      }
+      LAUNCH(s, k_lowrank_schur, (int64_t)m * m, m, s->Q1, is_nt(s) ? s->Q1 : s->Q2, b.sg, H);
+    } else if (!b.dense) {
       LAUNCH(s, k_schur_pairs, (int64_t)m * (m + 1) / 2, m, b.conptr, b.erow, b.ecol, b.eval, n, L, R, H);
     } else if (is_nt(s)) {
       // P = [A_1; ...; A_m] G (rows (j, r)), then B_j = (A_j G)' G, then
@@ -1603,6 +1681,27 @@ int tc_setup(S* s, bool mixed) {
       CU(s, cudaMemcpy(b.kmap, km.data(), sizeof(int2) * km.size(), cudaMemcpyHostToDevice));
     }
   }
+  int64_t lr_bytes = 0;
+  for (auto& b : s->B) {
+    if (!b.lowrank) continue;
+    const int n = b.n;
+    lr_bytes = std::max(lr_bytes, std::max(tcg::sliced_bytes(n, m, 7), tcg::sliced_bytes(m, n, 7)));
+    for (int mi = 0; mi < nmodes; ++mi) {
+      const int nsl = mi ? 3 : 7;
+      void* mem = tcalloc(tcg::sliced_bytes(m, n, nsl));
+      if (!mem) return 1;
+      CU(s, tcg::sliced_init(&b.vk[mi], mem, m, n, nsl, s->st));
+      tc_slice(s, op_rows(b.V, n, true, m, n), &b.vk[mi]);  // row j = v_j
+    }
+    void* mem = tcalloc(tcg::sliced_bytes(n, m, 7));
+    if (!mem) return 1;
+    CU(s, tcg::sliced_init(&b.vr, mem, n, m, 7, s->st));
+    tc_slice(s, op_rows(b.V, n, false, n, m), &b.vr);  // row r = (v_1r ... v_mr)
+  }
+  if (lr_bytes) {
+    s->tLm = tcalloc(lr_bytes);
+    if (!s->tLm) return 1;
+  }
   if (ns && m) {
     for (int mi = 0; mi < nmodes; ++mi) {
       const int nsl = mi ? 3 : 7;
@@ -1614,6 +1713,68 @@ int tc_setup(S* s, bool mixed) {
   }
   CU(s, cudaStreamSynchronize(s->st));
   return s->fail ? 1 : 0;
+}
+
+// Every constraint of the block is sg_j v_j v_j' (or zero): fills V
+// (n x m, column-major) and sg from the coordinate lists (v_j from the
+// column of the largest diagonal entry); false when any entry differs from
+// sg_j v_rj v_cj by more than 8 eps of the constraint's largest entry, or
+// when an entry of the outer product is missing.
+bool detect_rank_one(int n, int m, int64_t nnz, const int32_t* con, const int32_t* row, const int32_t* col,
+                     const double* val, std::vector<double>* V, std::vector<double>* sg) {
+  std::vector<int64_t> start(m + 2, 0);
+  bool grouped = true;  // entries already in constraint order (the usual input): no permutation
+  for (int64_t e = 0; e < nnz; ++e) {
+    if (con[e] < 0 || con[e] >= m || row[e] < 0 || row[e] >= n || col[e] < 0 || col[e] >= n) return false;
+    start[con[e] + 2] += 1;
+    grouped = grouped && (e == 0 || con[e] >= con[e - 1]);
+  }
+  for (int j = 0; j < m; ++j) start[j + 2] += start[j + 1];
+  std::vector<int64_t> ord;
+  if (grouped) {
+    for (int j = 0; j <= m; ++j) start[j] = start[j + 1];
+  } else {
+    ord.resize(nnz);
+    for (int64_t e = 0; e < nnz; ++e) ord[start[con[e] + 1]++] = e;
+  }
+  auto at = [&](int64_t q) { return grouped ? q : ord[q]; };
+  V->assign((size_t)n * m, 0.0);
+  sg->assign(m, 1.0);
+  std::vector<double> w(n);
+  for (int j = 0; j < m; ++j) {
+    const int64_t e0 = start[j], e1 = start[j + 1];
+    if (e0 == e1) continue;
+    int p = -1;
+    double dmax = 0.0, amax = 0.0;
+    for (int64_t q = e0; q < e1; ++q) {
+      const int64_t e = at(q);
+      amax = std::max(amax, std::fabs(val[e]));
+      if (row[e] == col[e] && std::fabs(val[e]) > dmax) { dmax = std::fabs(val[e]); p = row[e]; }
+    }
+    if (p < 0 || !(dmax > 0.0) || !std::isfinite(amax)) return false;
+    double dp = 0.0;
+    for (int64_t q = e0; q < e1; ++q) {
+      const int64_t e = at(q);
+      if (row[e] == p && col[e] == p) dp = val[e];
+    }
+    const double scale = std::sqrt(std::fabs(dp)), sgn = dp > 0 ? 1.0 : -1.0;
+    std::fill(w.begin(), w.end(), 0.0);
+    for (int64_t q = e0; q < e1; ++q) {
+      const int64_t e = at(q);
+      if (col[e] == p) w[row[e]] = val[e] / scale;
+    }
+    int64_t k = 0;
+    for (double v : w) k += v != 0.0;
+    if (e1 - e0 != k * k) return false;
+    for (int64_t q = e0; q < e1; ++q) {
+      const int64_t e = at(q);
+      const double wr = w[row[e]], wc = w[col[e]];
+      if (wr == 0.0 || wc == 0.0 || std::fabs(sgn * wr * wc - val[e]) > 8.0 * kEps * amax) return false;
+    }
+    std::copy(w.begin(), w.end(), V->begin() + (int64_t)j * n);
+    (*sg)[j] = sgn;
+  }
+  return true;
 }
 
 void release(S* s) {
@@ -1681,6 +1842,8 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   s->B.resize(s->nb);
   double cmax = 0.0;
   int64_t dense_ws = 0;
+  std::vector<std::vector<double>> lrV(s->nb), lrS(s->nb);
+  bool any_lowrank = false;
   for (int i = 0; i < s->nb; ++i) {
     Blk& b = s->B[i];
     b.n = d->sides[i];
@@ -1689,7 +1852,13 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
     const double n = b.n;
     const double pair_cost = (double)b.nnz * (double)b.nnz;
     const double dense_cost = 4.0 * n * n * n * m + 2.0 * (double)m * m * n * n;
-    b.dense = m > 0 && pair_cost > dense_cost && n * n * m * 8.0 * 3.0 < 96e9;
+    // rank-one constraints (LowRankOpt's low-rank format): products with
+    // V = [v_1 ... v_m] when cheaper than entry pairs and dense products
+    const double lowrank_cost = 4.0 * n * n * m + 2.0 * (double)m * m * n;
+    b.lowrank = m > 0 && lowrank_cost < std::min(pair_cost, dense_cost) &&
+                detect_rank_one(b.n, m, b.nnz, d->A_con[i], d->A_row[i], d->A_col[i], d->A_val[i], &lrV[i], &lrS[i]);
+    any_lowrank = any_lowrank || b.lowrank;
+    b.dense = !b.lowrank && m > 0 && pair_cost > dense_cost && n * n * m * 8.0 * 3.0 < 96e9;
     if (b.dense) dense_ws = std::max<int64_t>(dense_ws, (int64_t)b.n * b.n * m);
   }
   // ---- device allocations
@@ -1700,6 +1869,10 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   s->corrlin = vec(ns); s->vlin = vec(ns); s->ctv = vec(ns); s->wlin = vec(ns);
   s->H = vec((int64_t)m * m); s->H0 = vec((int64_t)m * m);
   s->ir_r = vec(m); s->ir_d = vec(m); s->ir_h = vec(m);
+  if (any_lowrank) {
+    s->Q1 = vec((int64_t)m * m); s->Q2 = vec((int64_t)m * m);
+    if (!s->Q1 || !s->Q2) return bail(MSDP_ERR_OUT_OF_MEMORY);
+  }
   if (dense_ws) { s->Tb = vec(dense_ws); s->Bb = vec(dense_ws); }
   {
     int64_t nn_dense = 0;
@@ -1749,7 +1922,12 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
     b.cnorm = cn;
     cmax = std::max(cmax, cn);
     CU(s, cudaMemcpy(b.C, d->C[i], 8 * nn, cudaMemcpyHostToDevice));
-    if (b.dense) {
+    if (b.lowrank) {
+      b.V = vec((int64_t)n * m); b.sg = vec(m); b.P = vec((int64_t)n * m);
+      if (!b.V || !b.sg || !b.P) return bail(MSDP_ERR_OUT_OF_MEMORY);
+      CU(s, cudaMemcpy(b.V, lrV[i].data(), 8 * lrV[i].size(), cudaMemcpyHostToDevice));
+      CU(s, cudaMemcpy(b.sg, lrS[i].data(), 8 * lrS[i].size(), cudaMemcpyHostToDevice));
+    } else if (b.dense) {
       std::vector<double> Ad((size_t)nn * m, 0.0);
       for (int64_t e = 0; e < b.nnz; ++e) Ad[(size_t)con[e] * nn + row[e] + (int64_t)col[e] * n] += val[e];
       b.Aall = vec(nn * m);
@@ -1935,7 +2113,8 @@ int msdp_solver_schur_assemble(msdp_solver* s, int32_t precision, double* H) {
   if (!s || (s->m && !H) || (precision != MSDP_FP64 && precision != MSDP_MIXED)) return MSDP_ERR_INVALID_ARGUMENT;
   if (precision == MSDP_MIXED && !is_nt(s)) return MSDP_ERR_UNSUPPORTED;
   if (precision == MSDP_MIXED &&
-      std::any_of(s->B.begin(), s->B.end(), [](const Blk& b) { return b.dense && !b.stk[1].s; }))
+      std::any_of(s->B.begin(), s->B.end(),
+                  [](const Blk& b) { return (b.dense && !b.stk[1].s) || (b.lowrank && !b.vk[1].s); }))
     return MSDP_ERR_UNSUPPORTED;  // split-precision slices are made for mixed-precision solvers only
   s->fail = 0;
   if (!s->m) return MSDP_OK;

@@ -131,16 +131,46 @@ def dense_random(sides, ns: int, m: int, seed: int = 0) -> Model:
     Cs, As = [], []
     b = np.zeros(m)
     for n in sides:
-        G = rng.standard_normal((m, n, n)) / np.sqrt(n)
-        Aj = (G + G.transpose(0, 2, 1)) / np.sqrt(2.0)
+        Aj = rng.standard_normal((m, n, n)) / np.sqrt(n)
+        Aj += Aj.transpose(0, 2, 1)
+        Aj /= np.sqrt(2.0)
         b += np.einsum("jaa->j", Aj)
         Cs.append(np.einsum("j,jab->ab", y0, Aj) + np.eye(n))
+        # entries in (constraint, column, row) order, the order the model
+        # keeps (Aj is exactly symmetric, so Aj[j, c, r] is entry (r, c))
+        jj = np.repeat(np.arange(m, dtype=np.int32), n * n)
+        cc = np.tile(np.repeat(np.arange(n, dtype=np.int32), n), m)
+        rr = np.tile(np.arange(n, dtype=np.int32), m * n)
+        As.append(BlockConstraints(n, m, jj, rr, cc, Aj.ravel()))
+        del Aj
+    C_lin = rng.standard_normal((m, ns))
+    b += C_lin.sum(axis=1)
+    d_lin = C_lin.T @ y0 + 1.0
+    Cs = [(c + c.T) / 2 for c in Cs]
+    return Model(Cs, As, b, d_lin, C_lin)
+
+
+def rank_one_random(sides, ns: int, m: int, seed: int = 0) -> Model:
+    """Rank-one constraint matrices A_ij = s_ij v_ij v_ij' (LowRankOpt's
+    low-rank format), v_ij with N(0, 1/n_i) entries and signs s_ij = +-1,
+    feasible by construction as in dense_random: X0 = I, x0 = 1,
+    y0 ~ N(0, 1), S0 = I, z0 = 1."""
+    rng = np.random.default_rng(seed)
+    y0 = rng.standard_normal(m)
+    Cs, As = [], []
+    b = np.zeros(m)
+    for n in sides:
+        Vm = rng.standard_normal((n, m)) / np.sqrt(n)
+        sg = rng.choice([-1.0, 1.0], m)
+        Aj = np.einsum("j,aj,bj->jab", sg, Vm, Vm)
+        b += np.einsum("jaa->j", Aj)
+        C = np.einsum("j,jab->ab", y0, Aj) + np.eye(n)
+        Cs.append((C + C.T) / 2)
         jj, rr, cc = np.meshgrid(np.arange(m), np.arange(n), np.arange(n), indexing="ij")
         As.append(BlockConstraints(n, m, jj.ravel(), rr.ravel(), cc.ravel(), Aj.ravel()))
     C_lin = rng.standard_normal((m, ns))
     b += C_lin.sum(axis=1)
     d_lin = C_lin.T @ y0 + 1.0
-    Cs = [(c + c.T) / 2 for c in Cs]
     return Model(Cs, As, b, d_lin, C_lin)
 
 

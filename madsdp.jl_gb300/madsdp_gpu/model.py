@@ -34,31 +34,38 @@ class BlockConstraints:
     """Coordinate list of the symmetric matrices ``A_ij`` of one block."""
 
     def __init__(self, n: int, m: int, con, row, col, val):
-        con = np.asarray(con, dtype=np.int64)
-        row = np.asarray(row, dtype=np.int64)
-        col = np.asarray(col, dtype=np.int64)
+        con = np.asarray(con)
+        row = np.asarray(row)
+        col = np.asarray(col)
         val = np.asarray(val, dtype=np.float64)
         if not (con.shape == row.shape == col.shape == val.shape):
             raise ValueError("coordinate arrays must have the same length")
         keep = val != 0.0
-        con, row, col, val = con[keep], row[keep], col[keep], val[keep]
+        if not keep.all():
+            con, row, col, val = con[keep], row[keep], col[keep], val[keep]
         if con.size and (con.min() < 0 or con.max() >= m):
             raise ValueError("constraint index out of range")
         if row.size and (min(row.min(), col.min()) < 0 or max(row.max(), col.max()) >= n):
             raise ValueError("entry index out of range")
-        order = np.lexsort((row, col, con))
         self.n = int(n)
         self.m = int(m)
+        # (constraint, column, row) order; input already in that order (the
+        # generators' and a column-major walk's) is kept without a sort
+        key = (con.astype(np.int64) * n + col) * n + row
+        if key.size < 2 or bool(np.all(key[1:] >= key[:-1])):
+            order = slice(None)
+        else:
+            order = np.argsort(key, kind="stable")
+        del key
         # int32 indices and contiguous values: the layout the C ABI reads,
         # so that a batch passes these arrays to it without copies
-        self.con = con[order].astype(np.int32)
-        self.row = row[order].astype(np.int32)
-        self.col = col[order].astype(np.int32)
+        self.con = np.ascontiguousarray(con[order], dtype=np.int32)
+        self.row = np.ascontiguousarray(row[order], dtype=np.int32)
+        self.col = np.ascontiguousarray(col[order], dtype=np.int32)
         self.val = np.ascontiguousarray(val[order])
         # constraint pointer (CSR over constraints)
         self.ptr = np.zeros(m + 1, dtype=np.int64)
-        np.add.at(self.ptr, self.con + 1, 1)
-        self.ptr = np.cumsum(self.ptr)
+        self.ptr[1:] = np.cumsum(np.bincount(self.con, minlength=m))
 
     @property
     def nnz(self) -> int:

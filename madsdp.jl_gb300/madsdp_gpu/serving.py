@@ -294,15 +294,26 @@ def _dense_request(rng, nmin: int, nmax: int, mmax: int, seed: int, mmin: int = 
 
 
 def poisson_stream(rate: float, duration: float, seed: int = 0, sos_d=(5, 63), maxcut_n=(20, 64),
-                   dense_n=(8, 24), dense_m=60, dense_m_min: int = 10) -> List[Tuple[float, str, Model]]:
+                   dense_n=(8, 24), dense_m=60, dense_m_min: int = 10,
+                   dense_pool: Optional[int] = None) -> List[Tuple[float, str, Model]]:
     """(arrival time, kind, model) for Poisson arrivals at `rate` per second.
 
     The mix is 50% SOS lower bounds (Gram side d+1, d ~ U(sos_d)), 30% max-cut
     (n ~ U(maxcut_n), edge probability 4/n) and 20% random dense SDPs (one
     block n ~ U(dense_n), m ~ U(dense_m_min, dense_m) capped at n(n+1)/2, no
     scalars; the cap keeps the constraint map of full rank).
+
+    dense_pool = K draws the dense requests from K models generated up front
+    with that distribution (each arrival picks one at random): a dense
+    request with n = 256 and m = 3000 holds about 1.5 GB of constraint data,
+    so a stream of hundreds of distinct ones does not fit host memory.
     """
     rng = np.random.default_rng(seed)
+    pool = None
+    if dense_pool:
+        prng = np.random.default_rng(seed + 7919)
+        pool = [_dense_request(prng, dense_n[0], dense_n[1], dense_m, seed * 1000003 + 999000 + k, dense_m_min)
+                for k in range(dense_pool)]
     t, out, k = 0.0, [], 0
     while True:
         t += rng.exponential(1.0 / rate)
@@ -316,7 +327,10 @@ def poisson_stream(rate: float, duration: float, seed: int = 0, sos_d=(5, 63), m
             n = int(rng.integers(maxcut_n[0], maxcut_n[1] + 1))
             out.append((t, "maxcut", g.maxcut(n, min(1.0, 4.0 / n), seed=s)))
         else:
-            out.append((t, "dense", _dense_request(rng, dense_n[0], dense_n[1], dense_m, s, dense_m_min)))
+            if pool is not None:
+                out.append((t, "dense", pool[int(rng.integers(len(pool)))]))
+            else:
+                out.append((t, "dense", _dense_request(rng, dense_n[0], dense_n[1], dense_m, s, dense_m_min)))
         k += 1
     return out
 

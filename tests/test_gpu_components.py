@@ -24,8 +24,9 @@ def oracle_after(model, iterations=2):
     return s
 
 
-@pytest.mark.parametrize("model", [g.dense_random([30, 12], 6, 60, seed=3), g.maxcut(40, 0.2, seed=2)],
-                         ids=["dense_scalars", "maxcut"])
+@pytest.mark.parametrize("model", [g.dense_random([30, 12], 6, 60, seed=3), g.maxcut(40, 0.2, seed=2),
+                                   g.rank_one_random([30, 20], 4, 50, seed=9)],
+                         ids=["dense_scalars", "maxcut", "rank_one"])
 def test_prepare_and_assembly_match_oracle(gpu_ctx, model):
     ref = oracle_after(model)
     inst = M.InstanceSolver(model)

@@ -203,3 +203,22 @@ def test_mixed_config3_full_size(gpu_ctx, config3):
     s = inst(model, precision="mixed")
     assert_matches_oracle(s, ref, traj=False)
     assert s.stats["iter_fp32"] >= 1
+
+
+# ---------------------------------------------------------------- rank-one constraints
+# LowRankOpt's low-rank format (README.md:137-152 of the reference): every
+# A_j = s_j v_j v_j' is detected at upload and applied through V = [v_1 ...
+# v_m] (H = s s' o (V'WV) o (V'WV) for NT, A(X)_j = s_j v_j'Xv_j,
+# A*(y) = V diag(s y) V').
+@pytest.mark.parametrize("direction", ["NT", "HKM"])
+def test_rank_one_constraints_match_oracle(gpu_ctx, direction):
+    model = g.rank_one_random([40, 25], 8, 60, seed=5)
+    s = inst(model, direction=getattr(M, direction)())
+    ref = o.Solver(model, direction=getattr(o, direction)()).solve()
+    assert_matches_oracle(s, ref)
+
+
+def test_rank_one_constraints_mixed(gpu_ctx):
+    model = g.rank_one_random([60], 0, 120, seed=6)
+    s = inst(model, precision="mixed")
+    assert_matches_oracle(s, o.Solver(model).solve(), traj=False)
