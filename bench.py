@@ -714,7 +714,9 @@ def run_gpu(args):
     if args.serve_seconds > 0:
         from madsdp_gpu.serving import Server, poisson_stream, serve_stream
         mix = SERVE_MIXES[args.serve_mix]
-        stream = poisson_stream(args.serve_rate, args.serve_seconds, seed=args.seed + 17 + rank, **mix)
+        pool = args.serve_dense_pool if args.serve_mix == "stated" else None
+        stream = poisson_stream(args.serve_rate, args.serve_seconds, seed=args.seed + 17 + rank, dense_pool=pool,
+                                **mix)
         srv = Server(memory_budget_bytes=8 << 30, max_slots=4096, precision="mixed", context=ctx,
                      whole_gpu_slots=args.serve_whole_gpu_slots, whole_gpu_memory_bytes=64 << 30)
         serving = serve_stream(srv, stream, iterations=args.serve_iterations, time_limit=1800.0,
@@ -724,6 +726,9 @@ def run_gpu(args):
                         "iterations_per_wave": args.serve_iterations, "wave_budget_ms": args.serve_budget_ms,
                         "memory_budget_bytes": 8 << 30, "whole_gpu_slots": args.serve_whole_gpu_slots,
                         "whole_gpu_memory_bytes": 64 << 30, "mix_name": args.serve_mix,
+                        "dense_requests": ("drawn from %d dense models generated before the stream (each up to "
+                                           "1.5 GB of constraint data); every request is solved in full" % pool)
+                        if pool else "one model per request",
                         "mix": "50%% SOS d~U%s, 30%% max-cut n~U%s p=4/n, 20%% dense one block n~U%s "
                                "m~U(%d, %d) capped at n(n+1)/2; requests with a block above 64 or m above 300 run "
                                "in whole-GPU slots" % (mix["sos_d"], mix["maxcut_n"], mix["dense_n"],
@@ -809,7 +814,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-mix", default="stated", choices=sorted(SERVE_MIXES))
-    ap.add_argument("--serve-whole-gpu-slots", type=int, default=4)
+    ap.add_argument("--serve-whole-gpu-slots", type=int, default=8)
+    ap.add_argument("--serve-dense-pool", type=int, default=6)
     ap.add_argument("--serve-iterations", type=int, default=1000)
     ap.add_argument("--serve-budget-ms", type=float, default=20.0)
     ap.add_argument("--workload", default="sos_batch", choices=["sos_batch", *INSTANCE_WORKLOADS])
