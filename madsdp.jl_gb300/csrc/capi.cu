@@ -587,7 +587,10 @@ int msdp_batch_get_all_solutions(msdp_batch* b, double* out) {
     solution_segments(b, &segs, &total);
     CK(cudaMalloc((void**)&b->gsol, sizeof(double) * (size_t)std::max<int64_t>(total, 1)));
     CK(cudaMalloc(&b->gseg, sizeof(SolSeg) * std::max<size_t>(segs.size(), 1)));
-    CK(cudaMemcpy(b->gseg, segs.data(), sizeof(SolSeg) * segs.size(), cudaMemcpyHostToDevice));
+    // on the batch's stream (the gather below reads the segments there);
+    // the pageable source lives until the copy has completed
+    CK(cudaMemcpyAsync(b->gseg, segs.data(), sizeof(SolSeg) * segs.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     b->nseg = (int64_t)segs.size();
     b->sol_size = total;
     b->bytes += sizeof(double) * total + sizeof(SolSeg) * segs.size();

@@ -117,6 +117,9 @@ __global__ void k_lin(int64_t N, double* out, double a, const double* A, double 
 }
 
 // A = (A + A')/2 in place (src/blocks.jl:77-84).
+// one double into device memory by kernel argument (no host source to keep alive)
+__global__ void k_put_scalar(double* p, double v) { *p = v; }
+
 __global__ void k_sym(int n, double* A) {
   const int64_t nn = (int64_t)n * n;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nn; idx += (int64_t)gridDim.x * blockDim.x) {
@@ -303,10 +306,8 @@ __global__ void k_aff_lin(int ns, double a, double b, const double* x, const dou
 
 // svec of m symmetric n x n matrices (column-major upper triangle,
 // off-diagonal entries times sqrt 2): <B_j, B_k> = svec(B_j) . svec(B_k)
-// lambda_min of formed symmetric matrices Z (n <= 128), one warp per
-// matrix: Lanczos with full reorthogonalization and Sturm bisection of the
-// tridiagonal (the routine of the per-problem kernel), basis in global
-// memory.  All eigenproblems of one step-length evaluation run in one launch.
+// One eigenproblem of a step-length evaluation (n x n basis, 4 (n + 1)
+// work entries, result slot).
 struct LanczosJob {
   int n;
   const double* Z;
@@ -315,17 +316,102 @@ struct LanczosJob {
   double* out;
 };
 
-__global__ void k_lanczos_batched(const LanczosJob* __restrict__ jobs) {
-  const LanczosJob j = jobs[blockIdx.x];
-  if (threadIdx.x < 32) {
-    double* a = j.ws;
-    double* bb = a + j.n + 1;
-    double* w = bb + j.n + 1;
-    double* coef = w + j.n + 1;
-    int steps = 0;
-    const double lam = warp_lanczos_eigmin<double>(j.n, j.Z, j.Q, 0, j.Q, a, bb, w, coef, &steps);
-    if (threadIdx.x == 0) *j.out = lam;
+// lambda_min of formed symmetric Z (n <= 256), one thread block of 256
+// threads per matrix: row i of each Lanczos vector on thread i, the basis in
+// global memory, full reorthogonalization twice (warp w forms the
+// coefficients of basis vectors w, w + 8, ...), and the stopping rule of the
+// one-warp routine of la.cuh: the smallest Ritz value of the tridiagonal
+// every 4 steps, stop once it moves by at most 64 eps max(1, |theta|) or the
+// Krylov space is exhausted.
+constexpr int kLanczosCta = 256;
+__device__ __forceinline__ double cta_sum256(double x, double* red) {
+  x = warp_sum(x);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+  __syncthreads();
+  double t = 0.0;
+#pragma unroll
+  for (int w = 0; w < kLanczosCta / 32; ++w) t += red[w];
+  __syncthreads();
+  return t;
+}
+__global__ void __launch_bounds__(kLanczosCta) k_lanczos_cta(const LanczosJob* __restrict__ jobs) {
+  const LanczosJob J = jobs[blockIdx.x];
+  const int n = J.n, i = threadIdx.x, lane = i & 31, wid = i >> 5;
+  __shared__ double qs[kLanczosCta], ws[kLanczosCta], coef[kLanczosCta + 1], red[kLanczosCta / 32];
+  __shared__ double theta_s;
+  double* a = J.ws;
+  double* bb = a + (n + 1);
+  double* Q = J.Q;
+  const bool own = i < n;
+  double v = 0.0;
+  if (own) {
+    uint32_t h = (uint32_t)(i + 1) * 2654435761u;
+    h ^= h >> 15; h *= 2246822519u; h ^= h >> 13;
+    v = (double)(h & 0xffffff) / 16777216.0 - 0.5 + 0.01;
   }
+  const double nrm = sqrt(cta_sum256(v * v, red));
+  if (own) {
+    v /= nrm;
+    Q[i] = v;
+    qs[i] = v;
+  }
+  if (i == 0) bb[0] = 0.0;
+  __syncthreads();
+  double theta = 0.0, theta_prev = INFINITY, znorm = 0.0;
+  for (int j = 0; j < n; ++j) {
+    double w = 0.0, w1 = 0.0;
+    if (own) {
+      int r = 0;
+      for (; r + 1 < n; r += 2) {
+        w = fma(J.Z[i + (int64_t)r * n], qs[r], w);
+        w1 = fma(J.Z[i + (int64_t)(r + 1) * n], qs[r + 1], w1);
+      }
+      if (r < n) w = fma(J.Z[i + (int64_t)r * n], qs[r], w);
+      w += w1;
+    }
+    const double aj = cta_sum256(own ? qs[i] * w : 0.0, red);
+    const double bj = j > 0 ? bb[j] : 0.0;
+    if (own) w -= aj * qs[i] + (j > 0 ? bj * Q[i + (int64_t)(j - 1) * n] : 0.0);
+    if (i == 0) a[j] = aj;
+    for (int pass = 0; pass < 2; ++pass) {
+      if (own) ws[i] = w;
+      __syncthreads();
+      for (int l = wid; l <= j; l += kLanczosCta / 32) {
+        const double* ql = Q + (int64_t)l * n;
+        double t = 0.0;
+        for (int r = lane; r < n; r += 32) t = fma(ql[r], ws[r], t);
+        t = warp_sum(t);
+        if (lane == 0) coef[l] = t;
+      }
+      __syncthreads();
+      if (own)
+        for (int l = 0; l <= j; ++l) w = fma(-coef[l], Q[i + (int64_t)l * n], w);
+    }
+    const double bn = sqrt(cta_sum256(own ? w * w : 0.0, red));
+    const int k = j + 1;
+    znorm = fmax(znorm, fabs(aj) + bn + fabs(bj));
+    if (i == 0) bb[j + 1] = bn;
+    const bool exhausted = (k == n) || !(bn > 2.220446049250313e-16 * znorm * 4.0);
+    if (exhausted || (k >= 4 && (k % 4) == 0)) {
+      __syncthreads();
+      if (wid == 0) {
+        const double th = warp_tridiag_eigmin<double>(k, a, bb);
+        if (lane == 0) theta_s = th;
+      }
+      __syncthreads();
+      theta = theta_s;
+      const double tolr = 2.220446049250313e-16 * 64.0 * fmax(1.0, fabs(theta));
+      if (exhausted || fabs(theta - theta_prev) <= tolr) break;
+      theta_prev = theta;
+    }
+    if (own) {
+      const double q = w / bn;
+      Q[i + (int64_t)(j + 1) * n] = q;
+      qs[i] = q;
+    }
+    __syncthreads();
+  }
+  if (i == 0) *J.out = theta;
 }
 
 // ---- coordinate-list constraints of one block
@@ -632,9 +718,29 @@ T* dalloc(S* s, int64_t count) {
   return (T*)p;
 }
 
+// Host data to the device on the solver's stream, complete on return (the
+// source may be pageable and short-lived; the legacy default stream is not
+// ordered with the solver's non-blocking stream, so no upload goes there).
+cudaError_t upload(S* s, void* dst, const void* src, size_t bytes) {
+  if (!bytes) return cudaSuccess;
+  const cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s->st);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(s->st);
+}
+
 // ---- reductions into slots
+// A fresh device scalar slot; past kSlots the solver fails instead of
+// writing beyond the slot arrays.
+int next_slot(S* s) {
+  if (s->nslot < kSlots) return s->nslot++;
+  if (!s->fail) {
+    s->fail = MSDP_ERR_CUDA;
+    s->err = "device scalar slots exhausted";
+  }
+  return kSlots - 1;
+}
+
 int reduce(S* s, int op, int64_t n, const double* a, const double* b = nullptr, int64_t stride = 1) {
-  const int slot = s->nslot++;
+  const int slot = next_slot(s);
   if (n <= 0) {
     LAUNCH(s, k_fill, 1, 1, s->slots + slot, (op == RED_MINRATIO || op == RED_MIN) ? INFINITY : 0.0);
     return slot;
@@ -646,7 +752,7 @@ int reduce(S* s, int op, int64_t n, const double* a, const double* b = nullptr, 
 }
 
 int copy_slot(S* s, const double* src) {
-  const int slot = s->nslot++;
+  const int slot = next_slot(s);
   CU(s, cudaMemcpyAsync(s->slots + slot, src, sizeof(double), cudaMemcpyDeviceToDevice, s->st));
   return slot;
 }
@@ -1208,16 +1314,16 @@ void correction(S* s) {
 }
 
 // ---- Lanczos for lambda_min of a formed symmetric Z (blocks above
-// kLanczosWarpMax).  Full reorthogonalization (twice); the step's scalars
+// kLanczosWarpMax, 256).  Full reorthogonalization (twice); the step's scalars
 // stay on the device and the host reads them every kLanczosBatch steps to
 // apply the stopping rule at each step in order: the smallest Ritz value of
 // the first step whose Ritz residual |beta_k s_k| is below 1e-12 ||Z||, or
 // of step n.  Gives up at kLanczosMax (the caller then uses the dense
 // eigensolver).
-constexpr int kLanczosMin = 129;
+constexpr int kLanczosMin = 257;
 constexpr int kLanczosMax = 320;
 constexpr int kLanczosBatch = 8;
-constexpr int kLanczosWarpMax = 128;  // batched one-warp device Lanczos up to this size
+constexpr int kLanczosWarpMax = kLanczosCta;  // batched one-block device Lanczos up to this size
 
 bool lanczos_eigmin(S* s, int n, const double* Z, double* out) {
   double* Q = s->lq;
@@ -1293,8 +1399,9 @@ int eigmin_large(S* s, Blk& b, double* Z) {
   if (n >= kLanczosMin) {
     double lam = 0.0;
     if (lanczos_eigmin(s, n, Z, &lam)) {
-      const int slot = s->nslot++;
-      CU(s, cudaMemcpyAsync(s->slots + slot, &lam, sizeof(double), cudaMemcpyHostToDevice, s->st));
+      const int slot = next_slot(s);
+      k_put_scalar<<<1, 1, 0, s->st>>>(s->slots + slot, lam);
+      s->launches += 1;
       return slot;
     }
   }
@@ -1362,7 +1469,7 @@ bool step_lengths(S* s, double* a_out, double* b_out) {
     }
     if (n <= kLanczosWarpMax) {
       for (int side = 0; side < 2; ++side) {
-        const int slot = s->nslot++;
+        const int slot = next_slot(s);
         jobs.push_back(LanczosJob{n, side ? b.T2 : b.T1, s->lq2 + qoff, s->lw2 + woff, s->slots + slot});
         qoff += (int64_t)n * n;
         woff += 4 * (int64_t)(n + 1);
@@ -1375,7 +1482,7 @@ bool step_lengths(S* s, double* a_out, double* b_out) {
   }
   if (!jobs.empty()) {
     CU(s, cudaMemcpyAsync(s->ljobs, jobs.data(), sizeof(LanczosJob) * jobs.size(), cudaMemcpyHostToDevice, s->st));
-    k_lanczos_batched<<<(unsigned)jobs.size(), 32, 0, s->st>>>((const LanczosJob*)s->ljobs);
+    k_lanczos_cta<<<(unsigned)jobs.size(), kLanczosCta, 0, s->st>>>((const LanczosJob*)s->ljobs);
     s->launches += 1;
   }
   const int rx = s->ns ? reduce(s, RED_MINRATIO, s->ns, s->x, s->dx) : -1;
@@ -1644,8 +1751,6 @@ int tc_setup(S* s, bool mixed) {
   CU(s, chol::init(&s->cw, cwm, nmax, s->terr, s->st));
   CU(s, chol::init(&s->cwH, cwh, std::max(m, 1), s->terr, s->st));
   CU(s, cudaMemsetAsync(s->hinfo_dev, 0, sizeof(int), s->st));
-  // the constraint data went up by synchronous copies from pageable memory
-  CU(s, cudaDeviceSynchronize());
   CU(s, cudaMemsetAsync(s->terr, 0, sizeof(int), s->st));
   const int nmodes = mixed ? 2 : 1;
   for (auto& b : s->B) {
@@ -1678,7 +1783,7 @@ int tc_setup(S* s, bool mixed) {
         for (int r = c; r < n; ++r) km.push_back(make_int2(r, c));
       b.kmap = (int2*)tcalloc((int64_t)sizeof(int2) * km.size());
       if (!b.kmap) return 1;
-      CU(s, cudaMemcpy(b.kmap, km.data(), sizeof(int2) * km.size(), cudaMemcpyHostToDevice));
+      CU(s, upload(s, b.kmap, km.data(), sizeof(int2) * km.size()));
     }
   }
   int64_t lr_bytes = 0;
@@ -1921,18 +2026,18 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
     for (int64_t k = 0; k < nn; ++k) cn = std::max(cn, std::fabs(d->C[i][k]));
     b.cnorm = cn;
     cmax = std::max(cmax, cn);
-    CU(s, cudaMemcpy(b.C, d->C[i], 8 * nn, cudaMemcpyHostToDevice));
+    CU(s, upload(s, b.C, d->C[i], 8 * nn));
     if (b.lowrank) {
       b.V = vec((int64_t)n * m); b.sg = vec(m); b.P = vec((int64_t)n * m);
       if (!b.V || !b.sg || !b.P) return bail(MSDP_ERR_OUT_OF_MEMORY);
-      CU(s, cudaMemcpy(b.V, lrV[i].data(), 8 * lrV[i].size(), cudaMemcpyHostToDevice));
-      CU(s, cudaMemcpy(b.sg, lrS[i].data(), 8 * lrS[i].size(), cudaMemcpyHostToDevice));
+      CU(s, upload(s, b.V, lrV[i].data(), 8 * lrV[i].size()));
+      CU(s, upload(s, b.sg, lrS[i].data(), 8 * lrS[i].size()));
     } else if (b.dense) {
       std::vector<double> Ad((size_t)nn * m, 0.0);
       for (int64_t e = 0; e < b.nnz; ++e) Ad[(size_t)con[e] * nn + row[e] + (int64_t)col[e] * n] += val[e];
       b.Aall = vec(nn * m);
       if (!b.Aall) return bail(MSDP_ERR_OUT_OF_MEMORY);
-      CU(s, cudaMemcpy(b.Aall, Ad.data(), 8 * Ad.size(), cudaMemcpyHostToDevice));
+      CU(s, upload(s, b.Aall, Ad.data(), 8 * Ad.size()));
     } else {
       const int64_t nnz = b.nnz;
       std::vector<int64_t> idx(nnz);
@@ -1964,14 +2069,14 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
       b.eval = vec(nnz); b.pval = vec(nnz);
       if (!b.conptr || !b.posptr || !b.erow || !b.ecol || !b.pcon || !b.eval || !b.pval)
         return bail(MSDP_ERR_OUT_OF_MEMORY);
-      CU(s, cudaMemcpy(b.conptr, cptr.data(), 8 * (m + 1), cudaMemcpyHostToDevice));
-      CU(s, cudaMemcpy(b.posptr, pptr.data(), 8 * (nn + 1), cudaMemcpyHostToDevice));
+      CU(s, upload(s, b.conptr, cptr.data(), 8 * (m + 1)));
+      CU(s, upload(s, b.posptr, pptr.data(), 8 * (nn + 1)));
       if (nnz) {
-        CU(s, cudaMemcpy(b.erow, er.data(), 4 * nnz, cudaMemcpyHostToDevice));
-        CU(s, cudaMemcpy(b.ecol, ec.data(), 4 * nnz, cudaMemcpyHostToDevice));
-        CU(s, cudaMemcpy(b.pcon, pc.data(), 4 * nnz, cudaMemcpyHostToDevice));
-        CU(s, cudaMemcpy(b.eval, ev.data(), 8 * nnz, cudaMemcpyHostToDevice));
-        CU(s, cudaMemcpy(b.pval, pv.data(), 8 * nnz, cudaMemcpyHostToDevice));
+        CU(s, upload(s, b.erow, er.data(), 4 * nnz));
+        CU(s, upload(s, b.ecol, ec.data(), 4 * nnz));
+        CU(s, upload(s, b.pcon, pc.data(), 4 * nnz));
+        CU(s, upload(s, b.eval, ev.data(), 8 * nnz));
+        CU(s, upload(s, b.pval, pv.data(), 8 * nnz));
       }
     }
   }
@@ -2006,9 +2111,9 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   for (int j = 0; j < m; ++j) bn = std::max(bn, std::fabs(d->b[j]));
   for (int k = 0; k < ns; ++k) dn = std::max(dn, std::fabs(d->d_lin[k]));
   s->bnorm = bn; s->dnorm = dn; s->cmax = cmax;
-  if (m) CU(s, cudaMemcpy(s->b, d->b, 8 * m, cudaMemcpyHostToDevice));
-  if (ns) CU(s, cudaMemcpy(s->dlin, d->d_lin, 8 * ns, cudaMemcpyHostToDevice));
-  if (ns && m) CU(s, cudaMemcpy(s->Clin, d->C_lin, 8 * (int64_t)m * ns, cudaMemcpyHostToDevice));
+  if (m) CU(s, upload(s, s->b, d->b, 8 * m));
+  if (ns) CU(s, upload(s, s->dlin, d->d_lin, 8 * ns));
+  if (ns && m) CU(s, upload(s, s->Clin, d->C_lin, 8 * (int64_t)m * ns));
   if (s->fail) return bail(s->fail);
   if (tc_setup(s, c.precision == MSDP_MIXED)) return bail(s->fail ? s->fail : MSDP_ERR_OUT_OF_MEMORY);
   *out = s;
@@ -2095,6 +2200,7 @@ int msdp_solver_set_iterate(msdp_solver* s, const double* const* X, const double
     CU(s, cudaMemcpyAsync(s->x, x, 8 * s->ns, cudaMemcpyHostToDevice, s->st));
     CU(s, cudaMemcpyAsync(s->z, z, 8 * s->ns, cudaMemcpyHostToDevice, s->st));
   }
+  CU(s, cudaStreamSynchronize(s->st));  // the caller's buffers are free again on return
   s->status = MSDP_REGULAR;
   if (!update_residuals(s)) return s->fail ? s->fail : MSDP_ERR_CUDA;
   return s->fail;
@@ -2155,11 +2261,12 @@ int msdp_solver_step_eig(msdp_solver* s, int32_t block, const double* L, const d
   CU(s, cudaMemcpyAsync(b.T2, D, 8 * nn, cudaMemcpyHostToDevice, s->st));
   form_congruence(s, n, b.T3, b.T2, b.T1);
   int slot;
+  LanczosJob job{};  // the copy's source: alive until fetch() below has synchronized
   if (n <= kLanczosWarpMax) {
-    slot = s->nslot++;
-    LanczosJob job{n, b.T1, s->lq2, s->lw2, s->slots + slot};
+    slot = next_slot(s);
+    job = LanczosJob{n, b.T1, s->lq2, s->lw2, s->slots + slot};
     CU(s, cudaMemcpyAsync(s->ljobs, &job, sizeof(job), cudaMemcpyHostToDevice, s->st));
-    k_lanczos_batched<<<1, 32, 0, s->st>>>((const LanczosJob*)s->ljobs);
+    k_lanczos_cta<<<1, kLanczosCta, 0, s->st>>>((const LanczosJob*)s->ljobs);
     s->launches += 1;
   } else {
     slot = eigmin_large(s, b, b.T1);

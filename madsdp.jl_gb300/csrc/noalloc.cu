@@ -203,6 +203,12 @@ extern "C" int msdp_solve_static(const msdp_problem_desc* prob, const msdp_compo
 
   // ---- upload (copies only) and zero what must start at zero
   cudaError_t e = cudaSuccess;
+  // an error return still waits for the copies in flight: their sources
+  // (this frame's descriptors, the caller's arrays) may be read until then
+  auto bail = [&]() {
+    cudaStreamSynchronize(st);
+    return MSDP_ERR_CUDA;
+  };
   auto up = [&](int64_t dst, const void* src, size_t bytes) {
     if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(base + dst, src, bytes, cudaMemcpyHostToDevice, st);
   };
@@ -222,7 +228,7 @@ extern "C" int msdp_solve_static(const msdp_problem_desc* prob, const msdp_compo
     up(o_rcol + sizeof(int32_t) * bd.ent, prob->A_col[i], sizeof(int32_t) * bd.nnz);
     up(o_rval + sizeof(double) * bd.ent, prob->A_val[i], sizeof(double) * bd.nnz);
   }
-  if (e != cudaSuccess) return MSDP_ERR_CUDA;
+  if (e != cudaSuccess) return bail();
 
   BatchDev B;
   std::memset(&B, 0, sizeof(B));
@@ -255,14 +261,14 @@ extern "C" int msdp_solve_static(const msdp_problem_desc* prob, const msdp_compo
   static_prepare_kernel<<<1, 32, 0, st>>>(B, (const int32_t*)(base + o_rcon), (const int32_t*)(base + o_rrow),
                                           (const int32_t*)(base + o_rcol), (const double*)(base + o_rval),
                                           (int64_t*)(base + o_cnt));
-  if (cudaGetLastError() != cudaSuccess) return MSDP_ERR_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return bail();
   // initialize!, then iterate to termination (the work queue starts at 0)
   prm.op = OP_INITIALIZE;
-  if (msdp_ipm_launch(0, B, 1, st) != cudaSuccess) return MSDP_ERR_CUDA;
-  if (cudaMemsetAsync(base + o_queue, 0, sizeof(int32_t), st) != cudaSuccess) return MSDP_ERR_CUDA;
+  if (msdp_ipm_launch(0, B, 1, st) != cudaSuccess) return bail();
+  if (cudaMemsetAsync(base + o_queue, 0, sizeof(int32_t), st) != cudaSuccess) return bail();
   prm.op = OP_ITERATE;
   prm.max_iterations = 0;
-  if (msdp_ipm_launch(0, B, 1, st) != cudaSuccess) return MSDP_ERR_CUDA;
+  if (msdp_ipm_launch(0, B, 1, st) != cudaSuccess) return bail();
 
   // ---- outputs
   double sc[SC_COUNT];
@@ -278,7 +284,7 @@ extern "C" int msdp_solve_static(const msdp_problem_desc* prob, const msdp_compo
     if (X) down(X[i], o_d64 + sizeof(double) * (bds[i].m64 + (int64_t)M_X * bds[i].n * bds[i].n),
                 sizeof(double) * bds[i].n * bds[i].n);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return MSDP_ERR_CUDA;
+  if (e != cudaSuccess) return bail();
   if ((int)sc[SC_STATUS] == MSDP_STATUS_INITIAL_POINT_ERROR) return MSDP_ERR_INITIAL_POINT;
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));

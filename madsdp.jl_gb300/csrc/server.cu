@@ -164,6 +164,10 @@ struct Wave {
   int32_t *dorder = nullptr, *dinit = nullptr, *queue = nullptr, *pending = nullptr;
   double* scal = nullptr;   // device scalars of the wave's requests
   double* hscal = nullptr;  // pinned host copy
+  // pinned staging of the wave's order and init lists and its pending
+  // count (capacity, capacity, 1): host->device copies read their source
+  // when the stream reaches them, and a wave is rewritten only once idle
+  int32_t* hlist = nullptr;
   std::vector<int32_t> slots;
   bool busy = false;
 };
@@ -216,6 +220,7 @@ void free_server(msdp_server* s) {
     if (w.stream) cudaStreamSynchronize(w.stream);
     cudaFree(w.dorder); cudaFree(w.dinit); cudaFree(w.queue); cudaFree(w.pending); cudaFree(w.scal);
     if (w.hscal) cudaFreeHost(w.hscal);
+    if (w.hlist) cudaFreeHost(w.hlist);
     if (w.done) cudaEventDestroy(w.done);
     if (w.stream) cudaStreamDestroy(w.stream);
   }
@@ -344,8 +349,13 @@ int step_async(msdp_server* s, int32_t iterations, double budget_s, int* done_no
     if (s->active[k] && s->active[k]->wave < 0) act.push_back(k);
   if (act.empty()) return MSDP_OK;
   const int mk = s->mixed ? 1 : 0;
+  int32_t* horder = w.hlist;
+  int32_t* hinit = w.hlist + s->capacity;
+  int32_t* hpend = w.hlist + 2 * s->capacity;
+  std::copy(act.begin(), act.end(), horder);
+  std::copy(fresh.begin(), fresh.end(), hinit);
   if (!fresh.empty()) {
-    e = cudaMemcpyAsync(w.dinit, fresh.data(), sizeof(int32_t) * fresh.size(), cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync(w.dinit, hinit, sizeof(int32_t) * fresh.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(w.queue, 0, sizeof(int32_t), st);
     BatchDev B = server_dev(s, w, w.dinit, (int)fresh.size());
     B.prm.op = OP_INITIALIZE;
@@ -354,15 +364,15 @@ int step_async(msdp_server* s, int32_t iterations, double budget_s, int* done_no
     s->launches += 1;
   }
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(w.dorder, act.data(), sizeof(int32_t) * act.size(), cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync(w.dorder, horder, sizeof(int32_t) * act.size(), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.queue, 0, sizeof(int32_t), st);
   BatchDev B = server_dev(s, w, w.dorder, (int)act.size());
   B.prm.op = OP_ITERATE;
   B.prm.max_iterations = iterations;
   B.prm.wave_ns = budget_s * 1e9;
   if (budget_s > 0.0) {
-    const int32_t cnt = (int32_t)act.size();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(w.pending, &cnt, sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    *hpend = (int32_t)act.size();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w.pending, hpend, sizeof(int32_t), cudaMemcpyHostToDevice, st);
     B.wave_pending = w.pending;
   }
   const int grid = std::min((int)act.size(), std::max(1, s->sm_count * s->occupancy));
@@ -430,7 +440,6 @@ int msdp_server_create(msdp_context* ctx, const msdp_components* comp, const msd
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->pval, sizeof(double) * s->entry_capacity);
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->dprob, sizeof(ProbDesc) * max_slots);
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->dblk, sizeof(BlockDesc) * max_slots * kMaxBlocks);
-  if (e == cudaSuccess) e = cudaMemset(s->dprob, 0, sizeof(ProbDesc) * max_slots);
   for (auto& w : s->waves) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming);
@@ -440,7 +449,12 @@ int msdp_server_create(msdp_context* ctx, const msdp_components* comp, const msd
     if (e == cudaSuccess) e = cudaMalloc((void**)&w.pending, sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMalloc((void**)&w.scal, sizeof(double) * SC_COUNT * max_slots);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&w.hscal, sizeof(double) * SC_COUNT * max_slots);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&w.hlist, sizeof(int32_t) * (2 * (size_t)max_slots + 1));
   }
+  // every request descriptor starts empty (on a server stream: the legacy
+  // default stream is not ordered with the non-blocking wave streams)
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->dprob, 0, sizeof(ProbDesc) * max_slots, s->waves[0].stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->waves[0].stream);
   if (e != cudaSuccess) {
     msdp_server* raw = s.release();
     free_server(raw);
