@@ -405,9 +405,11 @@ def run_instance(args):
         ms.append(e0.elapsed_time(e1))
     clocks = sampler.stop()
     launches = solver.launch_count - launches
+    counters = None
     if engine == "instance":
         st = solver.stats()
         phases = {k: round(v, 4) for k, v in solver.profile().items()}
+        counters = solver.counters()
     else:
         st = solver.stats(0)
         phases = None
@@ -469,6 +471,7 @@ def run_instance(args):
                    "tensor_core_assembly": tc_assembly,
                    "status": str(st["status"]), "iterations": st["iter"], "pobj": st["pobj"], "gap": st["gap"],
                    "inf_pr": st["inf_pr"], "inf_du": st["inf_du"], "phase_seconds_last_solve": phases,
+                   "work_counters_last_solve": counters,
                    "l2": f"{device_bytes / 2**20:.0f} MiB resident"},
         "gpu_launches": launches // max(1, args.steps),
         "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -730,8 +733,8 @@ def run_gpu(args):
                                            "1.5 GB of constraint data); every request is solved in full" % pool)
                         if pool else "one model per request",
                         "mix": "50%% SOS d~U%s, 30%% max-cut n~U%s p=4/n, 20%% dense one block n~U%s "
-                               "m~U(%d, %d) capped at n(n+1)/2; requests with a block above 64 or m above 300 run "
-                               "in whole-GPU slots" % (mix["sos_d"], mix["maxcut_n"], mix["dense_n"],
+                               "m~U(%d, %d) capped at n(n+1)/2; requests with a block above 128 or m above 300 run "
+                               "in whole-GPU slots (serve_whole_gpu)" % (mix["sos_d"], mix["maxcut_n"], mix["dense_n"],
                                                       mix["dense_m_min"], mix["dense_m"]),
                         "latency": "host clock, arrival to result available"})
         if rank == 0 and world == 1 and not args.no_cpu:

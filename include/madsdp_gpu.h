@@ -317,6 +317,13 @@ int64_t msdp_solver_device_bytes(const msdp_solver* solver);
  * residuals); returns the number of fields written. */
 int msdp_solver_get_profile(const msdp_solver* solver, double* seconds, int32_t capacity);
 const char* msdp_solver_profile_field_name(int32_t index);
+/* Work counters of the last msdp_solver_solve (no reference counterpart):
+   Schur refinement steps and FP64 fallbacks, NT eigendecompositions by FP32
+   eigensolver + FP64 refinement and by the dense FP64 eigensolver, the
+   refinement steps, tensor-core products.  Writes min(capacity, count)
+   values; returns that number. */
+int msdp_solver_get_counters(const msdp_solver* solver, int64_t* out, int32_t capacity);
+const char* msdp_solver_counter_name(int32_t index);
 /* Launches of this library's own kernels (library calls not counted). */
 int64_t msdp_solver_launch_count(const msdp_solver* solver);
 const char* msdp_solver_last_error(const msdp_solver* solver);

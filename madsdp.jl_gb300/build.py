@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libmadsdp_gpu.so")
-UNITS = ["kernel_fp64.cu", "kernel_mixed.cu", "capi.cu", "noalloc.cu", "server.cu", "instance.cu", "tcgemm.cu", "chol.cu", "schur.cu"]
+UNITS = ["kernel_fp64.cu", "kernel_mixed.cu", "capi.cu", "noalloc.cu", "server.cu", "instance.cu", "tcgemm.cu", "chol.cu", "schur.cu", "eigref.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -27,6 +27,7 @@
 
 #include "../../include/madsdp_gpu.h"
 #include "chol.h"
+#include "eigref.h"
 #include "la.cuh"
 #include "tcgemm.h"
 #include "tridiag.h"
@@ -634,6 +635,12 @@ struct msdp_solver {
   int64_t ir_steps = 0, ir_fallbacks = 0;
   double* work = nullptr;
   int lwork = 0;
+  // NT eigendecomposition by an FP32 eigensolver and FP64 refinement
+  // (eigref.h): FP32 matrix and eigenvalues, its workspace, index workspace
+  float *ef32 = nullptr, *ework32 = nullptr;
+  int elwork32 = 0;
+  int* eibuf = nullptr;
+  int64_t eig_refined = 0, eig_dense = 0, eig_steps = 0;
   double *lq = nullptr, *lh = nullptr;  // Lanczos basis (n x (kLanczosMax + 1)) and projections
   double *lq2 = nullptr, *lw2 = nullptr;  // bases and work of the batched device Lanczos
   void* ljobs = nullptr;
@@ -998,6 +1005,79 @@ bool update_termination(S* s) {
   return true;
 }
 
+// ---- NT eigendecomposition N = V diag(lam) V' (src/directions.jl:52-58)
+// Orders where cuSOLVER's FP32 eigensolver plus the refinement beat its
+// FP64 one on GB300 (measured: n = 100: 4.5 ms FP64 against 2.1 ms FP32;
+// n = 2000: 100 ms against 25 ms; n = 400: no gain).
+bool eig_refinable(int n) { return n >= 8 && (n <= 256 || n >= 600); }
+constexpr int kEigRefineMax = 8;
+// first-order corrections up to this size are taken; larger ones make
+// clusters.  cuSOLVER's FP32 eigenvectors at n = 2000 are orthogonal only
+// to about 2e-6 (measured on GB300; LAPACK's to 8e-9), and 1e-3 made
+// clusters of 70-210 vectors on max-cut iterates where 3e-2 makes at most 8
+// and converges in 4-5 steps.
+constexpr double kEigCouple = 3e-2;
+
+// FP32 eigenvectors (cuSOLVER's FP32 eigensolver on the shifted N; a
+// one-block FP32 Jacobi start measured slower at n = 100) refined to FP64
+// accuracy (eigref.h: Ogita-Aishima steps
+// with exact rotations inside clusters of close eigenvalues), every product
+// an FP64-accurate tensor-core product.  In: N's lower triangle in b.T2.
+// Out: V in b.T2, lam in b.lam (Rayleigh quotients, not sorted).  Returns
+// false when it did not converge or the FP32 solver failed; b.T2 then holds
+// N's lower triangle again.  The refinement works on N shifted by its mean
+// eigenvalue.  Scratch: b.G (N), b.W (shifted N, full), b.Gs, b.Si, b.Hx,
+// b.Gi, b.T3.
+bool nt_eig_refined(S* s, Blk& b) {
+  const int n = b.n;
+  const int64_t nn = (int64_t)n * n;
+  CU(s, cudaMemcpyAsync(b.G, b.T2, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s->st));  // N, for a fallback
+  CU(s, cudaMemcpyAsync(b.W, b.T2, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s->st));
+  LAUNCH(s, k_lower_to_full, nn, n, b.W);
+  // W = N - (trace N / n) I: same eigenvectors, eigenvalues shifted by the mean
+  const int tr = reduce(s, RED_SUM, n, b.W, nullptr, (int64_t)n + 1);
+  CU(s, eigref::shift_diag(n, b.W, s->slots + tr, -1.0 / n, s->st));
+  const int ke = next_info(s);
+  CU(s, eigref::to_float(nn, b.W, s->ef32, s->st));
+  CS(s, cusolverDnSsyevd(s->cs, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, s->ef32, n, s->ef32 + nn,
+                         s->ework32, s->elwork32, s->dinfo + ke));
+  CU(s, eigref::to_double(nn, s->ef32, b.T2, s->st));
+  s->launches += 3;
+  bool conv = false, ok = true;
+  for (int it = 0; it < kEigRefineMax && ok && !conv; ++it) {
+    gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.W, n, b.T2, n, 0.0, b.Gs, n);   // N V
+    gemm(s, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, 1.0, b.T2, n, b.Gs, n, 0.0, b.Si, n);  // S = V'NV
+    syrk(s, true, n, n, 1.0, b.T2, n, 0.0, b.Hx, n);                                  // R = V'V
+    // three consecutive slots for the residual measures of V
+    const int se = next_slot(s);
+    next_slot(s);
+    next_slot(s);
+    const int kf = next_info(s);
+    CU(s, cudaMemsetAsync(s->dinfo + kf, 0, sizeof(int), s->st));
+    CU(s, eigref::step(n, b.Si, b.Hx, kEigCouple, b.lam, b.Gi, s->eibuf, (unsigned long long*)(s->slots + se),
+                       s->dinfo + kf, s->st, &s->launches));
+    gemm(s, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, 1.0, b.T2, n, b.Gi, n, 0.0, b.T3, n);  // V (I + E)
+    CU(s, cudaMemcpyAsync(b.T2, b.T3, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s->st));
+    s->eig_steps += 1;
+    if (!fetch(s)) return false;
+    ok = s->hinfo[ke] == 0 && s->hinfo[kf] == 0 && se + 2 < kSlots;
+    // the basis this step started from was accurate to 1e-12 (off-diagonal
+    // residual relative to max |lam|, and orthogonality): after the step
+    // what remains is second order
+    const double lmax = s->hslots[se + 2];
+    const double off = lmax > 0.0 ? s->hslots[se] / lmax : (s->hslots[se] == 0.0 ? 0.0 : INFINITY);
+    const double res = std::max(off, s->hslots[se + 1]);
+    conv = ok && res <= 1e-12;
+  }
+  if (!conv) {
+    CU(s, cudaMemcpyAsync(b.T2, b.G, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s->st));
+    return false;
+  }
+  CU(s, eigref::shift_vec(n, b.lam, s->slots + tr, 1.0 / n, s->st));  // eigenvalues of N
+  s->launches += 3;
+  return true;
+}
+
 // ---- prepare (src/primal_dual.jl:29-37, src/directions.jl:45-75, src/blocks.jl:94-130)
 bool prepare(S* s, bool* ok) {
   reset_slots(s);
@@ -1021,10 +1101,15 @@ bool prepare(S* s, bool* ok) {
       // M = Ls' Lx ; N = M'M ; eig(N) = V diag(lam) V'
       gemm(s, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, 1.0, b.Ls, n, b.Lx, n, 0.0, b.T1, n);
       syrk(s, true, n, n, 1.0, b.T1, n, 0.0, b.T2, n);
-      const int ke = next_info(s);
-      CS(s, cusolverDnDsyevd(s->cs, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, b.T2, n, b.lam, s->work,
-                             s->lwork, s->dinfo + ke));
-      lam0.push_back(copy_slot(s, b.lam));
+      if (s->ef32 && eig_refinable(n) && nt_eig_refined(s, b)) {
+        s->eig_refined += 1;
+      } else {
+        const int ke = next_info(s);
+        CS(s, cusolverDnDsyevd(s->cs, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, b.T2, n, b.lam, s->work,
+                               s->lwork, s->dinfo + ke));
+        s->eig_dense += 1;
+      }
+      lam0.push_back(reduce(s, RED_MIN, n, b.lam));
       LAUNCH(s, k_nt_scaling, n, n, b.lam, b.D, b.sc);
       // G = Lx V D^-1/2 and W = G G'.  From M V = U D (U orthogonal):
       // Gi = G^-1 = D^-3/2 (M V)' Ls' (no triangular solve) and
@@ -2088,6 +2173,25 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   s->lwork = std::max(lwork, 1);
   s->work = vec(s->lwork);
   if (!s->work) return bail(MSDP_ERR_OUT_OF_MEMORY);
+  if (is_nt(s)) {
+    // FP32 eigensolver and refinement workspace of the NT eigendecomposition
+    int nref = 0, lw32 = 1;
+    for (auto& b : s->B) {
+      if (!eig_refinable(b.n)) continue;
+      nref = std::max(nref, b.n);
+      int lw = 0;
+      cusolverDnSsyevd_bufferSize(s->cs, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, b.n, nullptr, b.n,
+                                  nullptr, &lw);
+      lw32 = std::max(lw32, lw);
+    }
+    if (nref) {
+      s->ef32 = dalloc<float>(s, (int64_t)nref * nref + nref);  // FP32 matrix and eigenvalues
+      s->ework32 = dalloc<float>(s, lw32);
+      s->elwork32 = lw32;
+      s->eibuf = dalloc<int>(s, eigref::ibuf_ints(nref));
+      if (!s->ef32 || !s->ework32 || !s->eibuf) return bail(MSDP_ERR_OUT_OF_MEMORY);
+    }
+  }
   int nmax = 0;
   for (auto& b : s->B) nmax = std::max(nmax, b.n);
   if (nmax >= kLanczosMin) {
@@ -2148,6 +2252,7 @@ int msdp_solver_solve(msdp_solver* s) {
   s->mixed_on = s->comp.precision == MSDP_MIXED;
   s->n32 = s->n64 = 0;
   s->ir_steps = s->ir_fallbacks = 0;
+  s->eig_refined = s->eig_dense = s->eig_steps = 0;
   s->reg_used = 0.0;
   const double t0 = now_s();
   int rc = initialize(s);
@@ -2291,6 +2396,23 @@ int msdp_solver_get_profile(const msdp_solver* s, double* seconds, int32_t capac
 }
 
 const char* msdp_solver_profile_field_name(int32_t i) { return (i >= 0 && i < PH_COUNT) ? kPhaseNames[i] : nullptr; }
+
+namespace {
+const char* kCounterNames[] = {"refinement_steps", "refinement_fallbacks", "eig_refined", "eig_dense",
+                               "eig_refinement_steps", "tensor_core_products"};
+constexpr int kCounters = (int)(sizeof(kCounterNames) / sizeof(kCounterNames[0]));
+}  // namespace
+
+int msdp_solver_get_counters(const msdp_solver* s, int64_t* out, int32_t capacity) {
+  if (!s || !out) return MSDP_ERR_INVALID_ARGUMENT;
+  const int64_t v[kCounters] = {s->ir_steps, s->ir_fallbacks, s->eig_refined, s->eig_dense, s->eig_steps,
+                                s->tc_products};
+  const int n = std::min<int>(capacity, kCounters);
+  for (int k = 0; k < n; ++k) out[k] = v[k];
+  return n;
+}
+
+const char* msdp_solver_counter_name(int32_t i) { return (i >= 0 && i < kCounters) ? kCounterNames[i] : nullptr; }
 
 int64_t msdp_solver_device_bytes(const msdp_solver* s) { return s ? s->bytes : 0; }
 int64_t msdp_solver_launch_count(const msdp_solver* s) { return s ? s->launches : 0; }

@@ -115,6 +115,8 @@ SIGNATURES = [
     ("msdp_solver_device_bytes", i64, [C.c_void_p]),
     ("msdp_solver_get_profile", i32, [C.c_void_p, P(f64), i32]),
     ("msdp_solver_profile_field_name", C.c_char_p, [i32]),
+    ("msdp_solver_get_counters", i32, [C.c_void_p, P(i64), i32]),
+    ("msdp_solver_counter_name", C.c_char_p, [i32]),
     ("msdp_solver_launch_count", i64, [C.c_void_p]),
     ("msdp_solver_last_error", C.c_char_p, [C.c_void_p]),
     ("msdp_solver_set_iterate", i32, [C.c_void_p, P(P(f64)), P(P(f64)), P(f64), P(f64), P(f64)]),

@@ -21,11 +21,21 @@ from . import _lib, generators as g
 from .components import DenseCholesky, EigenStep, Mehrotra, NT, Options, PrimalDual, ScaledIdentity, Status
 from .model import Model
 from .solver import (Context, InstanceSolver, _Marshalled, _components, _options, _ptr, _stats_dict,
-                     _use_instance_engine, default_context)
+                     default_context)
 
-__all__ = ["Server", "poisson_stream", "serve_stream", "instance_bytes_estimate"]
+__all__ = ["Server", "poisson_stream", "serve_stream", "instance_bytes_estimate", "serve_whole_gpu"]
 
 LARGE_ID0 = 1 << 40  # request ids of whole-GPU requests start here
+
+
+def serve_whole_gpu(model: Model, batch_max_side: int = 128) -> bool:
+    """Whether a served request takes a whole-GPU slot.  For throughput the
+    rule is wider than MadSDPSolver's single-problem rule (blocks above 64):
+    a request whose blocks are at most `batch_max_side` and whose m is at
+    most 300 runs in the batched waves, one thread block among hundreds
+    resident at once, which serves many such requests at a time where a
+    whole-GPU solve of one of them leaves most of the GPU idle."""
+    return max(model.sides, default=0) > batch_max_side or model.m > 300
 
 
 def instance_bytes_estimate(model: Model) -> int:
@@ -135,15 +145,16 @@ class _WholeGPURequests:
 class Server:
     """A continuous-batching solve server on one GPU (msdp_server).
 
-    `whole_gpu_slots` > 0 adds a slot type for requests that the solver
-    would run on the whole GPU (a block above 64 or more than 300
-    constraints): they are solved by that many concurrent whole-GPU solvers,
-    admitted by `whole_gpu_memory_bytes`, beside the batched waves."""
+    `whole_gpu_slots` > 0 adds a slot type for requests too large for the
+    batched waves (`serve_whole_gpu`: a block above `batch_max_side` or more
+    than 300 constraints): they are solved by that many concurrent
+    whole-GPU solvers, admitted by `whole_gpu_memory_bytes`, beside the
+    batched waves."""
 
     def __init__(self, memory_budget_bytes: int = 1 << 30, max_slots: int = 1024, direction=None,
                  step=None, centering=None, initial_point=None, schur=None, precision: str = "fp64",
                  context: Optional[Context] = None, whole_gpu_slots: int = 0,
-                 whole_gpu_memory_bytes: int = 16 << 30, **options):
+                 whole_gpu_memory_bytes: int = 16 << 30, batch_max_side: int = 128, **options):
         self.ctx = context or default_context()
         self.lib = self.ctx.lib
         alg = PrimalDual(direction or NT(), step or EigenStep(), centering or Mehrotra())
@@ -158,6 +169,7 @@ class Server:
         self.h = h
         self.models: Dict[int, Model] = {}
         self.large = None
+        self.batch_max_side = int(batch_max_side)
         self._next_large = LARGE_ID0
         if whole_gpu_slots > 0:
             kw = dict(direction=alg.direction, step=alg.step, centering=alg.centering,
@@ -181,7 +193,7 @@ class Server:
             pass
 
     def submit(self, model: Model) -> int:
-        if self.large is not None and _use_instance_engine(model):
+        if self.large is not None and serve_whole_gpu(model, self.batch_max_side):
             rid = self._next_large
             self._next_large += 1
             self.models[rid] = model

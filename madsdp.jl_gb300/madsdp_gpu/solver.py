@@ -559,6 +559,14 @@ class InstanceSolver:
         n = self.lib.msdp_solver_get_profile(self.h, buf, 16)
         return {self.lib.msdp_solver_profile_field_name(i).decode(): buf[i] for i in range(max(n, 0))}
 
+    def counters(self) -> dict:
+        """Work counters of the last solve (refinement steps and fallbacks,
+        NT eigendecompositions by FP32 + refinement or dense FP64, tensor-core
+        products)."""
+        buf = (C.c_int64 * 16)()
+        n = self.lib.msdp_solver_get_counters(self.h, buf, 16)
+        return {self.lib.msdp_solver_counter_name(i).decode(): int(buf[i]) for i in range(max(n, 0))}
+
     def stats(self) -> dict:
         st = _lib.Stats()
         self.lib.msdp_solver_get_stats(self.h, C.byref(st))

@@ -70,6 +70,26 @@ def test_maxcut_pm1_weights_large(gpu_ctx):
     assert_matches_oracle(inst(model), o.Solver(model).solve())
 
 
+@pytest.mark.parametrize("n,refined", [(100, True), (400, False), (700, True)])
+def test_nt_eigendecomposition_refined(gpu_ctx, n, refined):
+    """The NT eigendecomposition N = V diag(lam) V' by the FP32 eigensolver
+    refined to FP64 accuracy with tensor-core products (orders where that is
+    faster than the FP64 eigensolver) or by the FP64 eigensolver: the same
+    trajectory as the oracle either way, and the counters show which ran."""
+    model = g.maxcut(n, 4.0 / n, weights="pm1", seed=n)
+    s = M.InstanceSolver(model)
+    s.solve()
+    c = s.counters()
+    st = s.stats()
+    s.close()
+    if refined:
+        assert c["eig_refined"] >= st["iter"] and c["eig_dense"] == 0, c
+        assert c["eig_refinement_steps"] <= 6 * c["eig_refined"], c
+    else:
+        assert c["eig_refined"] == 0 and c["eig_dense"] >= st["iter"], c
+    assert_matches_oracle(inst(model), o.Solver(model).solve())
+
+
 def test_lanczos_step_lengths_hkm(gpu_ctx):
     """Blocks of 257 and more take lambda_min by Lanczos; HKM exercises both
     the primal (Lx) and dual (Ls) congruences."""

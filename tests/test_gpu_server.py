@@ -186,7 +186,7 @@ def test_served_stated_mix_subsample_matches_oracle(gpu_ctx):
     import os
 
     import bench
-    from madsdp_gpu.solver import _use_instance_engine
+    from madsdp_gpu.serving import serve_whole_gpu
     from oracle import cpu_ipm
     stream = poisson_stream(200.0, 0.5, seed=29, **bench.SERVE_MIXES["stated"])
 
@@ -200,7 +200,7 @@ def test_served_stated_mix_subsample_matches_oracle(gpu_ctx):
     keep = [(k, m) for _, k, m in stream if cheap(k, m)][:24]
     kinds = [k for k, _ in keep]
     models = [m for _, m in keep]
-    large = [_use_instance_engine(m) for m in models]
+    large = [serve_whole_gpu(m) for m in models]
     assert any(l and k == "maxcut" for k, l in zip(kinds, large))
     assert any(l and k == "dense" for k, l in zip(kinds, large))
     ref = cpu_ipm.solve_many(models, threads=os.cpu_count() or 1)
