@@ -814,7 +814,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-mix", default="stated", choices=sorted(SERVE_MIXES))
     ap.add_argument("--serve-whole-gpu-slots", type=int, default=8)
