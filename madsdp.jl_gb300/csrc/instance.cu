@@ -819,9 +819,54 @@ tcg::Source op_rows(const double* Mp, int64_t ld, bool trans, int64_t rows, int6
 }
 
 // ---- dense linear algebra
+// Products whose dimensions are all at most kSmallGemm are one launch of a
+// plain FP64 kernel: at that size the tensor-core path's five launches
+// (row exponents and slices of both operands, then the product) cost more
+// time than the arithmetic.
+constexpr int kSmallGemm = 128;
+constexpr int kSgTile = 16;
+
+// C = alpha op(A) op(B) + beta C on CUDA cores (FP64), 16 x 16 output tiles
+// with both operand tiles staged in shared memory; lower: only i >= j.
+__global__ void __launch_bounds__(kSgTile * kSgTile)
+    k_dgemm_small(int m, int n, int k, int ta, int tb, double alpha, const double* __restrict__ A, int lda,
+                  const double* __restrict__ B, int ldb, double beta, double* C, int ldc, int lower) {
+  __shared__ double As[kSgTile][kSgTile + 1], Bs[kSgTile][kSgTile + 1];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = blockIdx.x * kSgTile + tx, j = blockIdx.y * kSgTile + ty;
+  double acc = 0.0;
+  for (int k0 = 0; k0 < k; k0 += kSgTile) {
+    // As[r][c] = op(A)(blockrow + r, k0 + c), Bs[r][c] = op(B)(k0 + r, blockcol + c)
+    {
+      const int r = tx, c = ty, gi = blockIdx.x * kSgTile + r, gk = k0 + c;
+      As[r][c] = (gi < m && gk < k) ? (ta ? A[gk + (int64_t)gi * lda] : A[gi + (int64_t)gk * lda]) : 0.0;
+      const int gk2 = k0 + tx, gj = blockIdx.y * kSgTile + ty;
+      Bs[tx][ty] = (gk2 < k && gj < n) ? (tb ? B[gj + (int64_t)gk2 * ldb] : B[gk2 + (int64_t)gj * ldb]) : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int l = 0; l < kSgTile; ++l) acc = fma(As[tx][l], Bs[l][ty], acc);
+    __syncthreads();
+  }
+  if (i < m && j < n && (!lower || i >= j)) {
+    double* c = C + i + (int64_t)j * ldc;
+    *c = beta == 0.0 ? alpha * acc : alpha * acc + beta * *c;
+  }
+}
+void small_gemm(S* s, int ta, int tb, int m, int n, int k, double alpha, const double* A, int lda, const double* B,
+                int ldb, double beta, double* C, int ldc, bool lower) {
+  const dim3 block(kSgTile, kSgTile), grid((m + kSgTile - 1) / kSgTile, (n + kSgTile - 1) / kSgTile);
+  k_dgemm_small<<<grid, block, 0, s->st>>>(m, n, k, ta, tb, alpha, A, lda, B, ldb, beta, C, ldc, lower ? 1 : 0);
+  s->launches += 1;
+}
+
 // C = alpha op(A) op(B) + beta C (FP64-accurate tensor-core product)
 void gemm(S* s, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k, double alpha, const double* A, int lda,
           const double* Bm, int ldb, double beta, double* C, int ldc) {
+  if (m <= kSmallGemm && n <= kSmallGemm && k <= kSmallGemm) {
+    small_gemm(s, ta != CUBLAS_OP_N, tb != CUBLAS_OP_N, m, n, k, alpha, A, lda, Bm, ldb, beta, C, ldc, false);
+    return;
+  }
   if (!tc_bind(s, &s->tA, s->tAm, m, k, 7) || !tc_bind(s, &s->tB, s->tBm, n, k, 7)) return;
   tc_slice(s, op_rows(A, lda, ta != CUBLAS_OP_N, m, k), &s->tA);
   tc_slice(s, op_rows(Bm, ldb, tb == CUBLAS_OP_N, n, k), &s->tB);
@@ -829,6 +874,11 @@ void gemm(S* s, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
 }
 // lower triangle of C = alpha op(A) op(A)' + beta C, op(A) n x k
 void syrk(S* s, bool trans, int n, int k, double alpha, const double* A, int lda, double beta, double* C, int ldc) {
+  if (n <= kSmallGemm && k <= kSmallGemm) {
+    // op(A) op(A)': op(A) = A' when trans
+    small_gemm(s, trans ? 1 : 0, trans ? 0 : 1, n, n, k, alpha, A, lda, A, lda, beta, C, ldc, true);
+    return;
+  }
   if (!tc_bind(s, &s->tA, s->tAm, n, k, 7)) return;
   tc_slice(s, op_rows(A, lda, trans, n, k), &s->tA);
   tc_product(s, s->tA, s->tA, tcg::kFp64, C, ldc, alpha, beta, true);
