@@ -149,12 +149,16 @@ class Server:
     batched waves (`serve_whole_gpu`: a block above `batch_max_side` or more
     than 300 constraints): they are solved by that many concurrent
     whole-GPU solvers, admitted by `whole_gpu_memory_bytes`, beside the
-    batched waves."""
+    batched waves.  They run in `whole_gpu_precision` (FP64 by default: on
+    the whole GPU the FP64 products are tensor-core products already, and
+    the split-precision Schur solve with refinement measured slower; None
+    takes `precision`)."""
 
     def __init__(self, memory_budget_bytes: int = 1 << 30, max_slots: int = 1024, direction=None,
                  step=None, centering=None, initial_point=None, schur=None, precision: str = "fp64",
                  context: Optional[Context] = None, whole_gpu_slots: int = 0,
-                 whole_gpu_memory_bytes: int = 16 << 30, batch_max_side: int = 128, **options):
+                 whole_gpu_memory_bytes: int = 16 << 30, batch_max_side: int = 128,
+                 whole_gpu_precision: Optional[str] = "fp64", **options):
         self.ctx = context or default_context()
         self.lib = self.ctx.lib
         alg = PrimalDual(direction or NT(), step or EigenStep(), centering or Mehrotra())
@@ -174,7 +178,7 @@ class Server:
         if whole_gpu_slots > 0:
             kw = dict(direction=alg.direction, step=alg.step, centering=alg.centering,
                       initial_point=initial_point or ScaledIdentity(), schur=schur or DenseCholesky(),
-                      precision=precision, **options)
+                      precision=whole_gpu_precision or precision, **options)
             self.large = _WholeGPURequests(whole_gpu_slots, whole_gpu_memory_bytes, self.ctx.device, kw)
         self.ctx.adopt(self)
 
