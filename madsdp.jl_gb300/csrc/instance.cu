@@ -24,6 +24,10 @@
 #include <numeric>
 #include <string>
 #include <vector>
+#include <atomic>
+#include <memory>
+#include <new>
+#include <thread>
 
 #include "../../include/madsdp_gpu.h"
 #include "chol.h"
@@ -1960,8 +1964,73 @@ int tc_setup(S* s, bool mixed) {
 // column of the largest diagonal entry); false when any entry differs from
 // sg_j v_rj v_cj by more than 8 eps of the constraint's largest entry, or
 // when an entry of the outer product is missing.
+// f(lo, hi) over the chunks of [0, count) on the host's threads (at most 32;
+// one when count is below `grain` per extra thread)
+template <class F>
+void host_parallel(int64_t count, F f, int64_t grain = (int64_t)1 << 20) {
+  const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+  const int64_t T = std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(hw, 32), count / std::max<int64_t>(grain, 1)));
+  if (T <= 1) {
+    f((int64_t)0, count);
+    return;
+  }
+  std::vector<std::thread> pool;
+  pool.reserve((size_t)T);
+  for (int64_t t = 0; t < T; ++t) pool.emplace_back(f, count * t / T, count * (t + 1) / T);
+  for (auto& th : pool) th.join();
+}
+
+// Whether the entries q in [e0, e1) (entry ord[q], or q without ord) of one
+// constraint are s v v' (every entry within 8 eps of s v_r v_c and no entry
+// of the outer product missing); v into w (length n) when w is given.
+bool rank_one_group(int n, int64_t e0, int64_t e1, const int64_t* ord, const int32_t* row, const int32_t* col,
+                    const double* val, double* w, double* sgn_out) {
+  auto at = [&](int64_t q) { return ord ? ord[q] : q; };
+  int p = -1;
+  double dmax = 0.0, amax = 0.0;
+  for (int64_t q = e0; q < e1; ++q) {
+    const int64_t e = at(q);
+    if (row[e] < 0 || row[e] >= n || col[e] < 0 || col[e] >= n) return false;
+    amax = std::max(amax, std::fabs(val[e]));
+    if (row[e] == col[e] && std::fabs(val[e]) > dmax) { dmax = std::fabs(val[e]); p = row[e]; }
+  }
+  if (p < 0 || !(dmax > 0.0) || !std::isfinite(amax)) return false;
+  double dp = 0.0;
+  for (int64_t q = e0; q < e1; ++q) {
+    const int64_t e = at(q);
+    if (row[e] == p && col[e] == p) dp = val[e];
+  }
+  const double scale = std::sqrt(std::fabs(dp)), sgn = dp > 0 ? 1.0 : -1.0;
+  std::vector<double> v(n, 0.0);
+  for (int64_t q = e0; q < e1; ++q) {
+    const int64_t e = at(q);
+    if (col[e] == p) v[row[e]] = val[e] / scale;
+  }
+  int64_t k = 0;
+  for (double x : v) k += x != 0.0;
+  if (e1 - e0 != k * k) return false;
+  for (int64_t q = e0; q < e1; ++q) {
+    const int64_t e = at(q);
+    const double wr = v[row[e]], wc = v[col[e]];
+    if (wr == 0.0 || wc == 0.0 || std::fabs(sgn * wr * wc - val[e]) > 8.0 * kEps * amax) return false;
+  }
+  if (w) std::copy(v.begin(), v.end(), w);
+  if (sgn_out) *sgn_out = sgn;
+  return true;
+}
+
 bool detect_rank_one(int n, int m, int64_t nnz, const int32_t* con, const int32_t* row, const int32_t* col,
                      const double* val, std::vector<double>* V, std::vector<double>* sg) {
+  // cheap rejection first: the leading run of entries of one constraint
+  // (grouped input) must itself be rank one, so dense or sparse general
+  // constraints are turned down without a pass over all entries (input
+  // whose constraints are not grouped may then miss the low-rank form and
+  // take the general paths, which give the same results)
+  if (nnz > 0 && con[0] >= 0 && con[0] < m) {
+    int64_t e1 = 0;
+    while (e1 < nnz && con[e1] == con[0]) ++e1;
+    if (!rank_one_group(n, 0, e1, nullptr, row, col, val, nullptr, nullptr)) return false;
+  }
   std::vector<int64_t> start(m + 2, 0);
   bool grouped = true;  // entries already in constraint order (the usual input): no permutation
   for (int64_t e = 0; e < nnz; ++e) {
@@ -1977,41 +2046,14 @@ bool detect_rank_one(int n, int m, int64_t nnz, const int32_t* con, const int32_
     ord.resize(nnz);
     for (int64_t e = 0; e < nnz; ++e) ord[start[con[e] + 1]++] = e;
   }
-  auto at = [&](int64_t q) { return grouped ? q : ord[q]; };
   V->assign((size_t)n * m, 0.0);
   sg->assign(m, 1.0);
-  std::vector<double> w(n);
   for (int j = 0; j < m; ++j) {
     const int64_t e0 = start[j], e1 = start[j + 1];
     if (e0 == e1) continue;
-    int p = -1;
-    double dmax = 0.0, amax = 0.0;
-    for (int64_t q = e0; q < e1; ++q) {
-      const int64_t e = at(q);
-      amax = std::max(amax, std::fabs(val[e]));
-      if (row[e] == col[e] && std::fabs(val[e]) > dmax) { dmax = std::fabs(val[e]); p = row[e]; }
-    }
-    if (p < 0 || !(dmax > 0.0) || !std::isfinite(amax)) return false;
-    double dp = 0.0;
-    for (int64_t q = e0; q < e1; ++q) {
-      const int64_t e = at(q);
-      if (row[e] == p && col[e] == p) dp = val[e];
-    }
-    const double scale = std::sqrt(std::fabs(dp)), sgn = dp > 0 ? 1.0 : -1.0;
-    std::fill(w.begin(), w.end(), 0.0);
-    for (int64_t q = e0; q < e1; ++q) {
-      const int64_t e = at(q);
-      if (col[e] == p) w[row[e]] = val[e] / scale;
-    }
-    int64_t k = 0;
-    for (double v : w) k += v != 0.0;
-    if (e1 - e0 != k * k) return false;
-    for (int64_t q = e0; q < e1; ++q) {
-      const int64_t e = at(q);
-      const double wr = w[row[e]], wc = w[col[e]];
-      if (wr == 0.0 || wc == 0.0 || std::fabs(sgn * wr * wc - val[e]) > 8.0 * kEps * amax) return false;
-    }
-    std::copy(w.begin(), w.end(), V->begin() + (int64_t)j * n);
+    double sgn = 1.0;
+    if (!rank_one_group(n, e0, e1, grouped ? nullptr : ord.data(), row, col, val, V->data() + (int64_t)j * n, &sgn))
+      return false;
     (*sg)[j] = sgn;
   }
   return true;
@@ -2151,12 +2193,26 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
     cusolverDnDpotri_bufferSize(s->cs, CUBLAS_FILL_MODE_LOWER, n, b.X, n, &lw); lwork = std::max(lwork, lw);
     cusolverDnDsyevd_bufferSize(s->cs, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, b.X, n, b.lam, &lw);
     lwork = std::max(lwork, lw);
-    // constraints
+    // constraints: range check on the host threads (tens of millions of
+    // entries for dense constraints), noting whether they come grouped by
+    // constraint
     const int32_t *con = d->A_con[i], *row = d->A_row[i], *col = d->A_col[i];
     const double* val = d->A_val[i];
-    for (int64_t e = 0; e < b.nnz; ++e)
-      if (con[e] < 0 || con[e] >= m || row[e] < 0 || row[e] >= n || col[e] < 0 || col[e] >= n)
-        return bail(MSDP_ERR_INVALID_ARGUMENT);
+    bool grouped = true;
+    {
+      std::atomic<bool> bad{false}, unordered{false};
+      host_parallel(b.nnz, [&](int64_t lo, int64_t hi) {
+        for (int64_t e = lo; e < hi; ++e) {
+          if (con[e] < 0 || con[e] >= m || row[e] < 0 || row[e] >= n || col[e] < 0 || col[e] >= n) {
+            bad = true;
+            return;
+          }
+          if (e > 0 && con[e] < con[e - 1]) unordered = true;
+        }
+      });
+      if (bad) return bail(MSDP_ERR_INVALID_ARGUMENT);
+      grouped = !unordered;
+    }
     double cn = 0.0;
     for (int64_t k = 0; k < nn; ++k) cn = std::max(cn, std::fabs(d->C[i][k]));
     b.cnorm = cn;
@@ -2168,11 +2224,27 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
       CU(s, upload(s, b.V, lrV[i].data(), 8 * lrV[i].size()));
       CU(s, upload(s, b.sg, lrS[i].data(), 8 * lrS[i].size()));
     } else if (b.dense) {
-      std::vector<double> Ad((size_t)nn * m, 0.0);
-      for (int64_t e = 0; e < b.nnz; ++e) Ad[(size_t)con[e] * nn + row[e] + (int64_t)col[e] * n] += val[e];
+      // A_j at [j n^2, (j+1) n^2); entries grouped by constraint are
+      // scattered by the host threads, each owning a range of constraints
+      // (so no two write the same A_j), else by one thread
+      const int64_t total = nn * m;
+      std::unique_ptr<double[]> Ad(new (std::nothrow) double[(size_t)std::max<int64_t>(total, 1)]);
+      if (!Ad) return bail(MSDP_ERR_OUT_OF_MEMORY);
+      auto scatter = [&](int c0, int c1) {
+        std::fill(Ad.get() + (int64_t)c0 * nn, Ad.get() + (int64_t)c1 * nn, 0.0);
+        const int64_t e0 = std::lower_bound(con, con + b.nnz, c0) - con;
+        const int64_t e1 = std::lower_bound(con, con + b.nnz, c1) - con;
+        for (int64_t e = e0; e < e1; ++e) Ad[(size_t)con[e] * nn + row[e] + (int64_t)col[e] * n] += val[e];
+      };
+      if (grouped) {
+        host_parallel(m, [&](int64_t lo, int64_t hi) { scatter((int)lo, (int)hi); }, 1);
+      } else {
+        host_parallel(total, [&](int64_t lo, int64_t hi) { std::fill(Ad.get() + lo, Ad.get() + hi, 0.0); });
+        for (int64_t e = 0; e < b.nnz; ++e) Ad[(size_t)con[e] * nn + row[e] + (int64_t)col[e] * n] += val[e];
+      }
       b.Aall = vec(nn * m);
       if (!b.Aall) return bail(MSDP_ERR_OUT_OF_MEMORY);
-      CU(s, upload(s, b.Aall, Ad.data(), 8 * Ad.size()));
+      CU(s, upload(s, b.Aall, Ad.get(), 8 * (size_t)total));
     } else {
       const int64_t nnz = b.nnz;
       std::vector<int64_t> idx(nnz);
