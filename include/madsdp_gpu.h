@@ -320,8 +320,10 @@ const char* msdp_solver_profile_field_name(int32_t index);
 /* Work counters of the last msdp_solver_solve (no reference counterpart):
    Schur refinement steps and FP64 fallbacks, NT eigendecompositions by FP32
    eigensolver + FP64 refinement and by the dense FP64 eigensolver, the
-   refinement steps, tensor-core products.  Writes min(capacity, count)
-   values; returns that number. */
+   refinement steps, tensor-core products, and for the step-length
+   lambda_min of blocks above 256 the Lanczos calls, their steps and the
+   calls that fell back to the dense eigensolver.  Writes min(capacity,
+   count) values; returns that number. */
 int msdp_solver_get_counters(const msdp_solver* solver, int64_t* out, int32_t capacity);
 const char* msdp_solver_counter_name(int32_t index);
 /* Launches of this library's own kernels (library calls not counted). */

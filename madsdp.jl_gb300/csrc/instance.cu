@@ -645,6 +645,7 @@ struct msdp_solver {
   int elwork32 = 0;
   int* eibuf = nullptr;
   int64_t eig_refined = 0, eig_dense = 0, eig_steps = 0;
+  int64_t lanczos_calls = 0, lanczos_steps = 0, eigmin_dense = 0;  // lambda_min of blocks above 256
   double *lq = nullptr, *lh = nullptr;  // Lanczos basis (n x (kLanczosMax + 1)) and projections
   double *lq2 = nullptr, *lw2 = nullptr;  // bases and work of the batched device Lanczos
   void* ljobs = nullptr;
@@ -1504,6 +1505,7 @@ bool lanczos_eigmin(S* s, int n, const double* Z, double* out) {
       LAUNCH(s, k_normalize, n, (int64_t)n, w, s->slots + sb, w);
     }
     if (!fetch(s)) return false;
+    s->lanczos_steps += k1 - k0;
     for (int k = k0; k < k1; ++k) {
       al.push_back(s->hslots[aslot[k]]);
       const double beta = std::sqrt(std::max(s->hslots[bslot[k]], 0.0));
@@ -1537,6 +1539,7 @@ int eigmin_large(S* s, Blk& b, double* Z) {
   const int n = b.n;
   if (n >= kLanczosMin) {
     double lam = 0.0;
+    s->lanczos_calls += 1;
     if (lanczos_eigmin(s, n, Z, &lam)) {
       const int slot = next_slot(s);
       k_put_scalar<<<1, 1, 0, s->st>>>(s->slots + slot, lam);
@@ -1547,6 +1550,7 @@ int eigmin_large(S* s, Blk& b, double* Z) {
   const int k = next_info(s);
   CS(s, cusolverDnDsyevd(s->cs, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_LOWER, n, Z, n, b.w, s->work, s->lwork,
                          s->dinfo + k));
+  s->eigmin_dense += 1;
   return copy_slot(s, b.w);
 }
 
@@ -2375,6 +2379,7 @@ int msdp_solver_solve(msdp_solver* s) {
   s->n32 = s->n64 = 0;
   s->ir_steps = s->ir_fallbacks = 0;
   s->eig_refined = s->eig_dense = s->eig_steps = 0;
+  s->lanczos_calls = s->lanczos_steps = s->eigmin_dense = 0;
   s->reg_used = 0.0;
   const double t0 = now_s();
   int rc = initialize(s);
@@ -2521,14 +2526,15 @@ const char* msdp_solver_profile_field_name(int32_t i) { return (i >= 0 && i < PH
 
 namespace {
 const char* kCounterNames[] = {"refinement_steps", "refinement_fallbacks", "eig_refined", "eig_dense",
-                               "eig_refinement_steps", "tensor_core_products"};
+                               "eig_refinement_steps", "tensor_core_products", "lanczos_calls", "lanczos_steps",
+                               "eigmin_dense"};
 constexpr int kCounters = (int)(sizeof(kCounterNames) / sizeof(kCounterNames[0]));
 }  // namespace
 
 int msdp_solver_get_counters(const msdp_solver* s, int64_t* out, int32_t capacity) {
   if (!s || !out) return MSDP_ERR_INVALID_ARGUMENT;
-  const int64_t v[kCounters] = {s->ir_steps, s->ir_fallbacks, s->eig_refined, s->eig_dense, s->eig_steps,
-                                s->tc_products};
+  const int64_t v[kCounters] = {s->ir_steps,    s->ir_fallbacks,  s->eig_refined,   s->eig_dense,   s->eig_steps,
+                                s->tc_products, s->lanczos_calls, s->lanczos_steps, s->eigmin_dense};
   const int n = std::min<int>(capacity, kCounters);
   for (int k = 0; k < n; ++k) out[k] = v[k];
   return n;
