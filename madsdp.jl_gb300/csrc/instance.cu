@@ -220,14 +220,6 @@ __global__ void k_div_rows(int n, double* A, const double* __restrict__ sc) {
 }
 
 // ---- Lanczos steps with the scalars kept on the device
-// w -= a q + b p with a = *pa and b = sqrt(*pbb) (the previous norm squared)
-__global__ void k_lanczos_update(int64_t n, double* __restrict__ w, const double* __restrict__ q,
-                                 const double* __restrict__ p, const double* __restrict__ pa,
-                                 const double* __restrict__ pbb) {
-  const double a = *pa, b = p ? sqrt(*pbb) : 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    w[i] -= a * q[i] + (p ? b * p[i] : 0.0);
-}
 // out[i] -= sum_j A[i + j lda] v[j]: 32 rows per block of 32 x 32 threads,
 // thread (r, g) sums columns g, g + 32, ... (coalesced over r); the 32
 // partial sums of a row are added in a fixed order
@@ -247,13 +239,91 @@ __global__ void __launch_bounds__(1024) k_gemv_sub(int64_t rows, int cols, const
     out[i] -= t;
   }
 }
-// out = w / sqrt(*pbb)
-__global__ void k_normalize(int64_t n, const double* __restrict__ w, const double* __restrict__ pbb,
-                            double* __restrict__ out) {
-  const double inv = 1.0 / sqrt(*pbb);
+// ---- one Lanczos step in fewer launches: each reduction leaves per-block
+// partial sums, and the kernel that needs the total sums them itself in a
+// fixed order (every block the same way), so results do not depend on
+// timing and no separate reduction launch is needed.
+__device__ __forceinline__ double block_sum256(double v, double* red) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+  __syncthreads();
+  return t;
+}
+// sum of np partials, identical in every block
+__device__ __forceinline__ double sum_partials(const double* __restrict__ part, int np, double* red) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) v += part[i];
+  return block_sum256(v, red);
+}
+// w = Z q (Z symmetric: column dots, one block per column as k_gemv_t) and
+// part[b] = sum of q_j w_j over the columns of block b
+__global__ void __launch_bounds__(kThreads) k_lz_matvec(int64_t n, const double* __restrict__ Z,
+                                                        const double* __restrict__ q, double* __restrict__ w,
+                                                        double* __restrict__ part) {
+  __shared__ double red[kThreads / 32];
+  double acc = 0.0;
+  for (int64_t j = blockIdx.x; j < n; j += gridDim.x) {
+    const double* a = Z + j * n;
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s = fma(a[i], q[i], s);
+    const double t = block_sum256(s, red);
+    if (threadIdx.x == 0) w[j] = t;
+    acc = fma(q[j], t, acc);
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+// a = sum of the matvec's partials (stored to *pa by block 0),
+// w -= a q + sqrt(*pbb) p (no p at the first step)
+__global__ void __launch_bounds__(kThreads) k_lz_update(int64_t n, double* __restrict__ w, const double* __restrict__ q,
+                                                        const double* __restrict__ p, const double* __restrict__ part,
+                                                        int np, double* __restrict__ pa,
+                                                        const double* __restrict__ pbb) {
+  __shared__ double red[kThreads / 32];
+  const double a = sum_partials(part, np, red);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *pa = a;
+  const double b = p ? sqrt(*pbb) : 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    w[i] -= a * q[i] + (p ? b * p[i] : 0.0);
+}
+// k_gemv_sub, and part[b] = sum of the updated out_i^2 over the block's rows
+__global__ void __launch_bounds__(1024) k_gemv_sub_dot(int64_t rows, int cols, const double* __restrict__ A,
+                                                      int64_t lda, const double* __restrict__ v,
+                                                      double* __restrict__ out, double* __restrict__ part) {
+  __shared__ double pr[32][33];
+  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int64_t i = (int64_t)blockIdx.x * 32 + r;
+  double s = 0.0;
+  if (i < rows)
+    for (int j = g; j < cols; j += 32) s = fma(A[i + j * lda], v[j], s);
+  pr[g][r] = s;
+  __syncthreads();
+  if (g == 0) {
+    double t = 0.0, sq = 0.0;
+    if (i < rows) {
+      for (int q = 0; q < 32; ++q) t += pr[q][r];
+      const double o = out[i] - t;
+      out[i] = o;
+      sq = o * o;
+    }
+    for (int o = 16; o; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    if (r == 0) part[blockIdx.x] = sq;
+  }
+}
+// bb = sum of the partials (stored to *pbb by block 0), out = w / sqrt(bb)
+__global__ void __launch_bounds__(kThreads) k_lz_normalize(int64_t n, const double* __restrict__ w,
+                                                           const double* __restrict__ part, int np,
+                                                           double* __restrict__ pbb, double* __restrict__ out) {
+  __shared__ double red[kThreads / 32];
+  const double bb = sum_partials(part, np, red);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *pbb = bb;
+  const double inv = 1.0 / sqrt(bb);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     out[i] = w[i] * inv;
 }
+int64_t lanczos_partials(int64_t n) { return std::min<int64_t>(n, 152 * 16) + (n + 31) / 32 + 1; }
 
 // out = -(M + M') ./ (D_i + D_j)  (src/directions.jl:90-100)
 __global__ void k_rnt(int n, const double* M, const double* D, double* out) {
@@ -647,6 +717,7 @@ struct msdp_solver {
   int64_t eig_refined = 0, eig_dense = 0, eig_steps = 0;
   int64_t lanczos_calls = 0, lanczos_steps = 0, eigmin_dense = 0;  // lambda_min of blocks above 256
   double *lq = nullptr, *lh = nullptr;  // Lanczos basis (n x (kLanczosMax + 1)) and projections
+  double* lzp = nullptr;                 // per-block partial sums of the fused Lanczos step
   double *lq2 = nullptr, *lw2 = nullptr;  // bases and work of the batched device Lanczos
   void* ljobs = nullptr;
   int* dinfo = nullptr;
@@ -1488,21 +1559,30 @@ bool lanczos_eigmin(S* s, int n, const double* Z, double* out) {
     for (int k = k0; k < k1; ++k) {
       const double* q = Q + (int64_t)k * n;
       double* w = Q + (int64_t)(k + 1) * n;
-      k_gemv_t<<<ga, kThreads, 0, s->st>>>(n, n, Z, n, q, w, 0);  // Z symmetric: Z'q = Zq
-      s->launches += 1;
-      const int sa = reduce(s, RED_DOT, n, q, w);
+      // seven launches per step: matvec with the a partials, update (sums
+      // them), two reorthogonalization passes (the second leaving the w'w
+      // partials), normalization (sums those)
+      double* pa_part = s->lzp;
+      double* pb_part = s->lzp + ga;
+      const int gsub = (n + 31) / 32;
+      const int sa = next_slot(s);
+      const int sb = next_slot(s);
       aslot.push_back(sa);
-      LAUNCH(s, k_lanczos_update, n, (int64_t)n, w, q, k ? Q + (int64_t)(k - 1) * n : nullptr, s->slots + sa,
-             k ? s->slots + bslot.back() : s->slots + sa);
+      k_lz_matvec<<<ga, kThreads, 0, s->st>>>((int64_t)n, Z, q, w, pa_part);
+      k_lz_update<<<grid_for(n), kThreads, 0, s->st>>>((int64_t)n, w, q, k ? Q + (int64_t)(k - 1) * n : nullptr,
+                                                        pa_part, ga, s->slots + sa,
+                                                        k ? s->slots + bslot.back() : s->slots + sa);
       for (int r = 0; r < 2; ++r) {
         k_gemv_t<<<std::min(k + 1, 152 * 16), kThreads, 0, s->st>>>(n, k + 1, Q, n, w, s->lh, 0);
-        s->launches += 1;
-        k_gemv_sub<<<(n + 31) / 32, 1024, 0, s->st>>>((int64_t)n, k + 1, Q, (int64_t)n, s->lh, w);
-        s->launches += 1;
+        if (r == 0)
+          k_gemv_sub<<<gsub, 1024, 0, s->st>>>((int64_t)n, k + 1, Q, (int64_t)n, s->lh, w);
+        else
+          k_gemv_sub_dot<<<gsub, 1024, 0, s->st>>>((int64_t)n, k + 1, Q, (int64_t)n, s->lh, w, pb_part);
       }
-      const int sb = reduce(s, RED_DOT, n, w, w);
       bslot.push_back(sb);
-      LAUNCH(s, k_normalize, n, (int64_t)n, w, s->slots + sb, w);
+      k_lz_normalize<<<grid_for(n), kThreads, 0, s->st>>>((int64_t)n, w, pb_part, gsub, s->slots + sb, w);
+      s->launches += 7;
+      CU(s, cudaGetLastError());
     }
     if (!fetch(s)) return false;
     s->lanczos_steps += k1 - k0;
@@ -2323,6 +2403,8 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   if (nmax >= kLanczosMin) {
     s->lq = vec((int64_t)nmax * (std::min(nmax, kLanczosMax) + 1));
     s->lh = vec(kLanczosMax + 1);
+    s->lzp = vec(lanczos_partials(nmax));
+    if (!s->lzp) return bail(MSDP_ERR_OUT_OF_MEMORY);
     if (!s->lq || !s->lh) return bail(MSDP_ERR_OUT_OF_MEMORY);
   }
   {
