@@ -325,6 +325,11 @@ __global__ void __launch_bounds__(kThreads) k_lz_normalize(int64_t n, const doub
 }
 int64_t lanczos_partials(int64_t n) { return std::min<int64_t>(n, 152 * 16) + (n + 31) / 32 + 1; }
 
+// 64-bit copy of sytrf's pivot indices (the solve's format)
+__global__ void k_ipiv64(int m, const int* __restrict__ p, int64_t* __restrict__ q) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) q[i] = p[i];
+}
+
 // out = -(M + M') ./ (D_i + D_j)  (src/directions.jl:90-100)
 __global__ void k_rnt(int n, const double* M, const double* D, double* out) {
   const int64_t nn = (int64_t)n * n;
@@ -700,6 +705,15 @@ struct msdp_solver {
   int64_t tc_products = 0;  // tensor-core products issued
   chol::Work cw, cwH;       // blocked Cholesky: blocks, and the Schur matrix (kept for its solves)
   int* hinfo_dev = nullptr; // status of the Schur factor
+  // MadNLPSchur: Bunch-Kaufman LDL' of the Schur matrix (cuSOLVER sytrf /
+  // sytrs, whose solve takes 64-bit pivot indices)
+  int* ipiv = nullptr;
+  int64_t* ipiv64 = nullptr;
+  double* sywork = nullptr;
+  int sylwork = 0;
+  void* sytrs_dev = nullptr;
+  size_t sytrs_dev_bytes = 0;
+  std::vector<char> sytrs_host;
   // mixed precision: split-precision assembly and FP32-class factor with
   // FP64 iterative refinement while `mixed_on`; FP64 after a stall
   bool mixed_on = false;
@@ -1028,6 +1042,7 @@ void jtprod(S* s, Blk& b, const double* yv, double* out) {
 }
 
 bool is_nt(const S* s) { return s->comp.direction == MSDP_NT; }
+bool is_madnlp(const S* s) { return s->comp.schur == MSDP_MADNLP_SCHUR; }
 
 // E(M): NT  W M W,  HKM  sym(X M S^-1)  (src/directions.jl:80-84,116-120)
 void apply_E(S* s, Blk& b, const double* M, double* out) {
@@ -1358,9 +1373,18 @@ bool factorize_schur(S* s, bool* ok, tcg::Mode mode) {
     CU(s, cudaMemcpyAsync(s->H, s->H0, sizeof(double) * m * m, cudaMemcpyDeviceToDevice, s->st));
     if (reg > 0) LAUNCH(s, k_add_diag, m, m, s->H, (int64_t)m, reg);
     const int nf = reduce(s, RED_NONFINITE, (int64_t)m * m, s->H);
-    note(s, chol::potrf(s->cwH, m, s->H, m, s->hinfo_dev, mode, s->st, &s->launches) == cudaSuccess, "chol::potrf");
     const int k = next_info(s);
-    CU(s, cudaMemcpyAsync(s->dinfo + k, s->hinfo_dev, sizeof(int), cudaMemcpyDeviceToDevice, s->st));
+    if (is_madnlp(s)) {
+      // MadNLPSchur (src/schur_solvers.jl:23-39, src/kkt.jl:7-32): Bunch-Kaufman
+      // LDL' of the lower triangle; fails on an exactly singular pivot
+      CS(s, cusolverDnDsytrf(s->cs, CUBLAS_FILL_MODE_LOWER, m, s->H, m, s->ipiv, s->sywork, s->sylwork,
+                             s->dinfo + k));
+      LAUNCH(s, k_ipiv64, m, m, s->ipiv, s->ipiv64);
+    } else {
+      note(s, chol::potrf(s->cwH, m, s->H, m, s->hinfo_dev, mode, s->st, &s->launches) == cudaSuccess,
+           "chol::potrf");
+      CU(s, cudaMemcpyAsync(s->dinfo + k, s->hinfo_dev, sizeof(int), cudaMemcpyDeviceToDevice, s->st));
+    }
     if (!fetch(s)) return false;
     if (s->hinfo[k] == 0 && s->hslots[nf] == 0.0) {
       s->reg_used = reg;
@@ -1382,6 +1406,12 @@ bool factorize_schur(S* s, bool* ok) { return factorize_schur(s, ok, s->mixed_on
 void chol_solve(S* s, const double* v, double* out) {
   const int m = s->m;
   if (out != v) CU(s, cudaMemcpyAsync(out, v, sizeof(double) * m, cudaMemcpyDeviceToDevice, s->st));
+  if (is_madnlp(s)) {
+    CS(s, cusolverDnXsytrs(s->cs, CUBLAS_FILL_MODE_LOWER, m, 1, CUDA_R_64F, s->H, m, s->ipiv64, CUDA_R_64F, out, m,
+                           s->sytrs_dev, s->sytrs_dev_bytes, s->sytrs_host.empty() ? nullptr : s->sytrs_host.data(),
+                           s->sytrs_host.size(), s->hinfo_dev));
+    return;
+  }
   note(s, chol::solve(s->cwH, m, s->H, m, out, s->hinfo_dev, s->st, &s->launches) == cudaSuccess, "chol::solve");
 }
 
@@ -2168,9 +2198,11 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
   if (comp) c = *comp; else msdp_default_components(&c);
   if (opt) o = *opt; else msdp_default_options(&o);
   if (d->nblocks < 0 || d->m < 0 || d->ns < 0 || (d->nblocks == 0 && d->ns == 0)) return MSDP_ERR_INVALID_ARGUMENT;
-  if (c.algorithm != MSDP_PRIMAL_DUAL || c.schur != MSDP_DENSE_CHOLESKY ||
+  if (c.algorithm != MSDP_PRIMAL_DUAL || (c.schur != MSDP_DENSE_CHOLESKY && c.schur != MSDP_MADNLP_SCHUR) ||
       (c.precision != MSDP_FP64 && c.precision != MSDP_FP64_TENSOR && c.precision != MSDP_MIXED))
     return MSDP_ERR_UNSUPPORTED;
+  // MadNLPSchur factors in FP64 only (no split-precision factor for it)
+  if (c.schur == MSDP_MADNLP_SCHUR && c.precision == MSDP_MIXED) return MSDP_ERR_UNSUPPORTED;
   // mixed: the refinement applies H matrix-free, which equals the factored
   // lower-triangle matrix only when H is symmetric (NT)
   if (c.precision == MSDP_MIXED && c.direction != MSDP_NT) return MSDP_ERR_UNSUPPORTED;
@@ -2375,6 +2407,22 @@ int msdp_solver_create(msdp_context* ctx, const msdp_problem_desc* d, const msdp
     int lw = 0;
     cusolverDnDpotrf_bufferSize(s->cs, CUBLAS_FILL_MODE_LOWER, m, s->H, m, &lw);
     lwork = std::max(lwork, lw);
+  }
+  if (m && c.schur == MSDP_MADNLP_SCHUR) {
+    int lw = 0;
+    if (cusolverDnDsytrf_bufferSize(s->cs, m, s->H, m, &lw) != CUSOLVER_STATUS_SUCCESS) return bail(MSDP_ERR_CUDA);
+    s->sylwork = std::max(lw, 1);
+    s->sywork = vec(s->sylwork);
+    s->ipiv = dalloc<int>(s, m);
+    s->ipiv64 = dalloc<int64_t>(s, m);
+    size_t dev = 0, host = 0;
+    if (cusolverDnXsytrs_bufferSize(s->cs, CUBLAS_FILL_MODE_LOWER, m, 1, CUDA_R_64F, s->H, m, s->ipiv64, CUDA_R_64F,
+                                    s->dy, m, &dev, &host) != CUSOLVER_STATUS_SUCCESS)
+      return bail(MSDP_ERR_CUDA);
+    s->sytrs_dev_bytes = std::max<size_t>(dev, 1);
+    s->sytrs_dev = dalloc<unsigned char>(s, (int64_t)s->sytrs_dev_bytes);
+    s->sytrs_host.assign(host, 0);
+    if (!s->sywork || !s->ipiv || !s->ipiv64 || !s->sytrs_dev) return bail(MSDP_ERR_OUT_OF_MEMORY);
   }
   s->lwork = std::max(lwork, 1);
   s->work = vec(s->lwork);

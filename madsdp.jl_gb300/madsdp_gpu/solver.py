@@ -12,14 +12,15 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import warnings
 import weakref
 from typing import List, Optional, Sequence
 
 import numpy as np
 
 from . import _lib
-from .components import (DenseCholesky, DualCentering, DualShift, EigenStep, InitialPoint, Mehrotra, NT,
-                         Options, PRECISIONS, PrimalDual, QRSchur, ScaledIdentity, Status)
+from .components import (DenseCholesky, DualCentering, DualShift, EigenStep, InitialPoint, MadNLPSchur, Mehrotra,
+                         NT, Options, PRECISIONS, PrimalDual, QRSchur, ScaledIdentity, Status)
 from .model import Model
 
 __all__ = ["Context", "Batch", "MadSDPSolver", "madsdp", "GPUError", "default_context"]
@@ -715,16 +716,26 @@ class MadSDPSolver:
         if engine not in ("auto", "batch", "instance"):
             raise ValueError("engine must be 'auto', 'batch' or 'instance'")
         if engine == "auto":
-            # the whole-GPU engine runs PrimalDual + DenseCholesky in FP64
+            # the whole-GPU engine runs PrimalDual with DenseCholesky (FP64,
+            # or mixed for NT) or MadNLPSchur (FP64)
             schur = kwargs.get("schur")
             prec = kwargs.get("precision", "fp64")
             alg = kwargs.get("algorithm")
             direction = kwargs.get("direction") or (alg.direction if isinstance(alg, PrimalDual) else None)
+            dense_chol = schur is None or isinstance(schur, DenseCholesky)
             supported = (not isinstance(alg, DualCentering)
-                         and (schur is None or isinstance(schur, DenseCholesky))
+                         and (dense_chol or isinstance(schur, MadNLPSchur))
                          and (prec in ("fp64", "fp64_tensor")
-                              or (prec == "mixed" and (direction is None or isinstance(direction, NT)))))
-            engine = "instance" if supported and (prec == "fp64_tensor" or _use_instance_engine(model)) else "batch"
+                              or (prec == "mixed" and dense_chol and (direction is None or isinstance(direction, NT)))))
+            large = _use_instance_engine(model)
+            engine = "instance" if supported and (prec == "fp64_tensor" or large) else "batch"
+            if large and not supported:
+                warnings.warn("this problem (largest block %d, m = %d) runs in one thread block: the whole-GPU "
+                              "engine does not take %s" % (max(model.sides, default=0), model.m,
+                                                          "DualCentering" if isinstance(alg, DualCentering)
+                                                          else type(schur).__name__ if not dense_chol
+                                                          else "mixed precision with HKM"),
+                              stacklevel=2)
         self.engine = engine
         self.batch = Batch([model], **kwargs) if engine == "batch" else None
         self.instance = InstanceSolver(model, **kwargs) if engine == "instance" else None

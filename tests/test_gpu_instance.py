@@ -158,6 +158,27 @@ def test_auto_engine_and_unsupported(gpu_ctx):
         M.InstanceSolver(g.maxcut(30, 0.2, seed=1), precision="mixed", direction=M.HKM())
     with pytest.raises(NotImplementedError):
         M.Batch([g.maxcut(30, 0.2, seed=1)], precision="fp64_tensor")
+    with pytest.raises(NotImplementedError):
+        M.InstanceSolver(g.maxcut(30, 0.2, seed=1), precision="mixed", schur=M.MadNLPSchur())
+    # a large problem with a component the whole-GPU engine does not take
+    # runs in one thread block, and says so
+    with pytest.warns(UserWarning, match="one thread block"):
+        s = M.MadSDPSolver(g.maxcut(100, 0.1, seed=1), schur=M.QRSchur())
+    assert s.engine == "batch"
+    s.close()
+    assert M.MadSDPSolver(g.maxcut(100, 0.1, seed=1), schur=M.MadNLPSchur()).engine == "instance"
+
+
+@pytest.mark.parametrize("direction,model", [("NT", g.maxcut(120, 0.05, seed=8)),
+                                             ("HKM", g.dense_random([40, 20], 30, 350, seed=9))])
+def test_madnlp_schur_on_the_whole_gpu(gpu_ctx, direction, model):
+    """MadNLPSchur (Bunch-Kaufman LDL' of the Schur matrix, src/kkt.jl:7-32,
+    src/schur_solvers.jl:23-39) on the whole-GPU engine: the same trajectory
+    as the oracle with the same component."""
+    s = inst(model, direction=getattr(M, direction)(), schur=M.MadNLPSchur())
+    assert s.engine == "instance"
+    ref = o.Solver(model, direction=getattr(o, direction)(), schur=o.MadNLPSchur()).solve()
+    assert_matches_oracle(s, ref)
 
 
 # ---------------------------------------------------------------- full sizes
